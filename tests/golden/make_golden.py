@@ -1,0 +1,216 @@
+"""Generate the golden fixtures under ``tests/golden/`` from the upstream code.
+
+Run in a container that holds the upstream PyTomography sources::
+
+    python tests/golden/make_golden.py            # writes tests/golden/*.npz
+
+Every output in the fixtures is produced by the upstream implementation itself
+(``SPECTSystemMatrix.forward/backward``, ``SPECTAttenuationTransform``,
+``SPECTPSFTransform``, ``PoissonLogLikelihood``, ``OSEM``, ``BSREM``,
+``RelativeDifferencePrior``, ``PETTOFMeta``, ``get_scanner_LUT``) imported
+through ``refharness``; only kornia's ``rotate`` is a restatement (see
+``refharness``).  Inputs are seeded and stored beside the outputs, so the tests
+never regenerate them.  Each SPECT case is run twice: in float32 (the
+reference's working precision) and in float64 (``pytomography.set_dtype``),
+which pins the float64 oracle.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import refharness  # noqa: E402
+
+pt = refharness.import_reference()
+from pytomography.metadata.SPECT import SPECTObjectMeta, SPECTProjMeta, SPECTPSFMeta  # noqa: E402
+from pytomography.projectors.SPECT import SPECTSystemMatrix  # noqa: E402
+from pytomography.transforms.SPECT import SPECTAttenuationTransform, SPECTPSFTransform  # noqa: E402
+from pytomography.likelihoods import PoissonLogLikelihood  # noqa: E402
+from pytomography.algorithms import OSEM, BSREM  # noqa: E402
+from pytomography.priors import RelativeDifferencePrior  # noqa: E402
+from pytomography.metadata.PET import PETTOFMeta  # noqa: E402
+from pytomography.io.PET import shared as pet_shared  # noqa: E402
+from pytomography.utils import compute_pad_size  # noqa: E402
+
+
+def set_precision(dt):
+    pt.set_dtype(dt)
+
+
+def ellipsoid_phantom(shape, dr, seed, n_ell=3):
+    """Small seeded phantom: background cylinder plus hot ellipsoids."""
+    g = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    x = (np.arange(nx) - (nx - 1) / 2) * dr[0]
+    y = (np.arange(ny) - (ny - 1) / 2) * dr[1]
+    z = (np.arange(nz) - (nz - 1) / 2) * dr[2]
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    rx, ry = 0.42 * nx * dr[0], 0.34 * ny * dr[1]
+    body = (X / rx) ** 2 + (Y / ry) ** 2 <= 1
+    f = 0.5 * body.astype(np.float64)
+    for _ in range(n_ell):
+        c = g.uniform(-0.5, 0.5, 3) * np.array([rx, ry, nz * dr[2] * 0.6])
+        a = g.uniform(0.15, 0.3, 3) * np.array([rx, ry, nz * dr[2]])
+        m = ((X - c[0]) / a[0]) ** 2 + ((Y - c[1]) / a[1]) ** 2 + ((Z - c[2]) / a[2]) ** 2 <= 1
+        f[m] = g.uniform(1, 10)
+    mu = np.where(body, 0.15, 0.0)
+    lung = ((X + 0.35 * rx) / (0.25 * rx)) ** 2 + (Y / (0.4 * ry)) ** 2 <= 1
+    mu = np.where(lung, 0.04, mu)
+    return f, mu
+
+
+def spect_case(name, shape, dr, angles, radii, variants, seed, out):
+    rng = np.random.default_rng(seed)
+    f_np, mu_np = ellipsoid_phantom(shape, dr, seed)
+    f_np = f_np + 0.1 * rng.random(shape)
+    g_np = rng.random((len(angles), shape[1], shape[2])) * 5
+    rec = {"shape": np.array(shape), "dr": np.array(dr), "angles": np.array(angles),
+           "radii": np.array(radii), "object": f_np, "mu": mu_np, "proj_in": g_np}
+    for prec, dt in (("f32", torch.float32), ("f64", torch.float64)):
+        set_precision(dt)
+        for var in variants:
+            om = SPECTObjectMeta(list(dr), tuple(shape))
+            pm = SPECTProjMeta((shape[1], shape[2]), list(dr[:2]), list(angles), radii=list(radii))
+            ts = []
+            for t in var.split("+"):
+                if t == "att":
+                    ts.append(SPECTAttenuationTransform(torch.tensor(mu_np, dtype=dt)))
+                elif t == "psf":
+                    ts.append(SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11))))
+                elif t == "psf1d":
+                    ts.append(SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11), kernel_dimensions="1D")))
+            H = SPECTSystemMatrix(ts, [], om, pm)
+            f = torch.tensor(f_np, dtype=dt)
+            g = torch.tensor(g_np, dtype=dt)
+            rec[f"fwd_{var}_{prec}"] = H.forward(f).numpy()
+            rec[f"bwd_{var}_{prec}"] = H.backward(g).numpy()
+            H.set_n_subsets(3)
+            rec[f"fwd_sub1_{var}_{prec}"] = H.forward(f, 1).numpy()
+            rec[f"bwd_sub1_{var}_{prec}"] = H.backward(H.get_projection_subset(g, 1), 1).numpy()
+            if prec == "f32":
+                for t in ts:
+                    if isinstance(t, SPECTPSFTransform):
+                        for r, layer in t.layers.items():
+                            key = f"psf_{var}_r{float(r):g}"
+                            rec[key + "_wr"] = layer.layer_r.weight.detach().numpy()[:, 0, :]
+                            if layer.layer_z is not None:
+                                rec[key + "_wz"] = layer.layer_z.weight.detach().numpy()[:, 0, :]
+    set_precision(torch.float32)
+    rec["variants"] = np.array(variants)
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **rec)
+    print("wrote", name)
+
+
+def osem_case(name, shape, dr, angles, radius, n_iters, n_subsets, seed, out,
+              bsrem=False, additive=False):
+    f_true, mu_np = ellipsoid_phantom(shape, dr, seed, n_ell=2)
+    rec = {"shape": np.array(shape), "dr": np.array(dr), "angles": np.array(angles),
+           "radii": np.full(len(angles), radius), "object_true": f_true, "mu": mu_np,
+           "n_iters": n_iters, "n_subsets": n_subsets}
+    set_precision(torch.float32)
+    om = SPECTObjectMeta(list(dr), tuple(shape))
+    pm = SPECTProjMeta((shape[1], shape[2]), list(dr[:2]), list(angles), radii=[radius] * len(angles))
+    att = SPECTAttenuationTransform(torch.tensor(mu_np, dtype=torch.float32))
+    psf = SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)))
+    H = SPECTSystemMatrix([att, psf], [], om, pm)
+    gen = torch.Generator().manual_seed(seed + 1)
+    clean = H.forward(torch.tensor(f_true, dtype=torch.float32)) * 20
+    g = torch.poisson(clean, generator=gen)
+    rec["projections"] = g.numpy()
+    s = None
+    if additive:
+        s = torch.full(g.shape, float(clean.mean()) * 0.1)
+        rec["additive"] = s.numpy()
+    iterates = []
+
+    class Keep:
+        def run(self, obj, n_iter, n_subset):
+            iterates.append(obj.clone().numpy())
+            return obj
+
+        def finalize(self, obj):
+            pass
+
+    lik = PoissonLogLikelihood(H, g, additive_term=s)
+    if bsrem:
+        prior = RelativeDifferencePrior(beta=0.3, gamma=2)
+        alg = BSREM(lik, prior=prior)
+        rec["beta"], rec["gamma"] = 0.3, 2.0
+    else:
+        alg = OSEM(lik)
+    alg(n_iters, n_subsets, callback=Keep())
+    rec["iterates"] = np.stack(iterates)
+    rec["norm_bps"] = np.stack([nb.numpy() for nb in lik.norm_BPs])
+    np.savez_compressed(os.path.join(out, f"{name}.npz"), **rec)
+    print("wrote", name)
+
+
+def rdp_case(out):
+    set_precision(torch.float32)
+    rng = np.random.default_rng(7)
+    shape = (10, 12, 9)
+    dr = (0.4, 0.4, 0.5)
+    f = rng.random(shape) * 5 + 0.01
+    f[2:4, 3:7, 1:5] = 0.0
+    prior = RelativeDifferencePrior(beta=0.3, gamma=2)
+    om = SPECTObjectMeta(list(dr), shape)
+    prior.set_object_meta(om)
+    prior.set_object(torch.tensor(f, dtype=torch.float32))
+    prior.set_beta_scale(0.25)
+    grad = prior(derivative_order=1).numpy()
+    value = prior(derivative_order=0)
+    np.savez_compressed(os.path.join(out, "rdp.npz"), object=f, dr=np.array(dr), beta=0.3,
+                        gamma=2.0, beta_scale=0.25, grad=grad, value=value)
+    print("wrote rdp")
+
+
+def pet_meta_case(out):
+    set_precision(torch.float32)
+    rec = {}
+    for nb, rng_mm, fwhm in ((13, 650.0, 58.5), (12, 600.0, 40.0)):
+        m = PETTOFMeta(nb, rng_mm, fwhm)
+        rec[f"tof_{nb}"] = np.array([float(m.bin_width), float(m.sigma), float(m.center_offset),
+                                     float(m.n_sigmas)])
+    info = dict(crystalTransNr=1, crystalTransSpacing=4.0, submoduleTransNr=1,
+                submoduleTransSpacing=0.0, moduleTransNr=1, moduleTransSpacing=0.0,
+                rsectorTransNr=60, crystalAxialNr=8, crystalAxialSpacing=4.0,
+                submoduleAxialNr=1, submoduleAxialSpacing=0.0, moduleAxialNr=1,
+                moduleAxialSpacing=0.0, rsectorAxialNr=1, radius=120.0,
+                firstCrystalAxis=1, NrCrystalsPerRing=60, NrRings=8)
+    rec["lut_small"] = pet_shared.get_scanner_LUT(info).numpy()
+    rec["lut_small_info"] = np.array([60, 8, 120.0, 4.0])
+    np.savez_compressed(os.path.join(out, "pet_meta.npz"), **rec)
+    print("wrote pet_meta")
+
+
+def main():
+    out = HERE
+    torch.manual_seed(0)
+    spect_case("spect_even", (16, 16, 12), (0.48, 0.48, 0.48),
+               [float(a) for a in np.linspace(0, 360, 11)[:-1]],
+               [25.0 if i % 2 == 0 else 21.0 for i in range(10)],
+               ["none", "att", "psf", "att+psf", "psf+att", "att+psf1d"], seed=11, out=out)
+    spect_case("spect_odd", (15, 15, 10), (0.442, 0.442, 0.5),
+               [3.7, 51.2, 97.0, 180.0, 222.5, 270.0, 333.3],
+               [22.0, 22.0, 19.0, 22.0, 23.5, 22.0, 19.0],
+               ["none", "att+psf"], seed=12, out=out)
+    osem_case("osem_small", (16, 16, 10), (0.48, 0.48, 0.48),
+              [float(a) for a in np.linspace(0, 360, 13)[:-1]], 20.0, 2, 3, seed=21, out=out)
+    osem_case("osem_additive", (14, 14, 8), (0.5, 0.5, 0.5),
+              [float(a) for a in np.linspace(0, 360, 9)[:-1]], 18.0, 2, 2, seed=22, out=out,
+              additive=True)
+    osem_case("bsrem_small", (16, 16, 10), (0.48, 0.48, 0.48),
+              [float(a) for a in np.linspace(0, 360, 13)[:-1]], 20.0, 2, 3, seed=23, out=out,
+              bsrem=True)
+    rdp_case(out)
+    pet_meta_case(out)
+    print("pad sizes", {n: compute_pad_size(n) for n in (15, 16, 64, 96, 128)})
+
+
+if __name__ == "__main__":
+    main()
