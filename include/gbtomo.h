@@ -1,0 +1,139 @@
+/*
+ * gbtomo — C ABI of the GB300 projector hot path (libgbtomo.so).
+ *
+ * Plain pointers and sizes only.  Every float pointer named "device" is a CUDA
+ * device pointer on the current device; streams are passed as opaque
+ * `gb_stream_t` (a cudaStream_t; NULL = legacy default stream).  All calls are
+ * stream-ordered and allocate nothing: plans own every table and scratch buffer
+ * they need, allocated at plan creation.  Calls on one plan must be ordered on a
+ * single stream (they share the plan's scratch).  Errors are negative status codes;
+ * gb_last_error() returns the message of the calling thread's last failure.
+ *
+ * The reference interfaces each entry point replaces are cited beside it
+ * (paths inside the PyTomography 3.3.2 source tree).
+ */
+#ifndef GBTOMO_H
+#define GBTOMO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t gb_status;
+typedef void *gb_stream_t;
+
+#define GB_OK 0
+#define GB_ERR_ARG (-1)          /* invalid argument / null pointer */
+#define GB_ERR_SHAPE (-2)        /* unsupported or inconsistent shape */
+#define GB_ERR_OOM (-3)          /* device allocation failed at plan creation */
+#define GB_ERR_CUDA (-4)         /* a CUDA runtime call or launch failed */
+#define GB_ERR_UNSUPPORTED (-5)  /* configuration outside what the kernels implement */
+#define GB_ERR_STATE (-6)        /* call out of order (e.g. subsets not set) */
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *gb_last_error(void);
+/* Library version string. */
+const char *gb_version(void);
+
+/* ------------------------------------------------------------------ SPECT */
+
+typedef struct gb_spect_plan gb_spect_plan;
+
+/* Geometry and plugin configuration of a SPECT rotate+sum system matrix.
+ * Mirrors SPECTObjectMeta / SPECTProjMeta (metadata/SPECT/spect_metadata.py:8-64),
+ * SPECTAttenuationTransform (transforms/SPECT/attenuation.py:24-115) and
+ * SPECTPSFTransform (transforms/SPECT/psf.py:101-231) after configure(). */
+typedef struct gb_spect_desc {
+    int32_t nx, ny, nz;       /* object shape [nx][ny][nz], z fastest; nx == ny */
+    float dx, dy, dz;         /* voxel size (cm) */
+    int32_t n_angles;         /* number of projection angles */
+    /* Normalised sampling matrices [n_angles][6] (host) of the kornia-convention
+     * in-plane rotation used by the forward projector (angle beta - 270) and the
+     * back-projector (angle 270 - beta): src = theta . (lin[col], lin[row], 1). */
+    const float *theta_fwd;
+    const float *theta_bwd;
+    const float *lin;         /* host [n_pad]: linspace(-1, 1, n_pad), n_pad = nx + 2*pad */
+    const float *mu;          /* device [nx][ny][nz] attenuation map (cm^-1), or NULL */
+    const char *order;        /* obj2obj transforms in application order: any of "", "a",
+                                 "p", "ap", "pa" (a = attenuation, p = PSF) */
+    int32_t psf_2d;           /* 1: blur along y and z ('2D'); 0: along y only ('1D') */
+    int32_t psf_n_groups;     /* number of distinct detector radii */
+    const int32_t *psf_group; /* host [n_angles]: PSF table index of each angle */
+    int32_t psf_k;            /* taps per table row (odd); shorter kernels are zero-padded */
+    const float *psf_taps_r;  /* host [n_groups][n_pad][psf_k]: y-direction taps per plane */
+    const float *psf_taps_z;  /* host [n_groups][n_pad][psf_k]: z-direction taps per plane */
+    float psf_trunc_rel;      /* taps below this fraction of a plane's largest tap are
+                                 dropped (0 keeps every tap) */
+} gb_spect_desc;
+
+/* Create / destroy a plan.  Creation uploads the geometry tables and precomputes the
+ * attenuation factors exp(-rev_cumsum(mu_rot*dx)) of every angle in the rotated
+ * padded frame (attenuation.py:11-21, utils/misc.py:8-19).  Replaces
+ * SPECTSystemMatrix.__init__ + Transform.configure
+ * (projectors/SPECT/spect_system_matrix.py:26-36, projectors/system_matrix.py:46-52). */
+gb_status gb_spect_plan_create(const gb_spect_desc *desc, gb_spect_plan **plan);
+gb_status gb_spect_plan_destroy(gb_spect_plan *plan);
+
+/* Interleaved angle subsets indices[i::n_subsets]
+ * (spect_system_matrix.py:58-71).  n_subsets >= 1. */
+gb_status gb_spect_set_subsets(gb_spect_plan *plan, int32_t n_subsets);
+/* Number of angles in a subset (-1 = all angles). */
+int32_t gb_spect_subset_size(const gb_spect_plan *plan, int32_t subset);
+
+/* Forward projection H_m f -> proj [n_sel][ny][nz] (device).
+ * Replaces SPECTSystemMatrix.forward (spect_system_matrix.py:120-157).
+ * subset = -1 projects every angle. */
+gb_status gb_spect_forward(gb_spect_plan *plan, const float *object, float *proj,
+                           int32_t subset, gb_stream_t stream);
+
+/* Back projection proj [n_sel][ny][nz] -> object [nx][ny][nz] (device, overwritten).
+ * adjoint = 0: the reference back-projector, which rotates back with bilinear
+ *              interpolation by +(270 - beta)
+ *              (SPECTSystemMatrix.backward, spect_system_matrix.py:159-201);
+ * adjoint = 1: the exact transpose of gb_spect_forward (same taps, scattered). */
+gb_status gb_spect_backward(gb_spect_plan *plan, const float *proj, float *object,
+                            int32_t subset, int32_t adjoint, gb_stream_t stream);
+
+/* One fused OSEM sub-iteration, in place on `object`:
+ *   f <- f + f/(normBP_m + delta) * (H_m^T (g_m / (H_m f + s_m + delta)) - normBP_m),
+ *   f[f <= 0] = 0.
+ * projections / additive are the FULL [n_angles][ny][nz] arrays (additive may be NULL);
+ * norm_bp is H_m^T 1 of this subset.  Replaces one pass of
+ * PreconditionedGradientAscentAlgorithm.__call__ with OSEM
+ * (algorithms/preconditioned_gradient_ascent.py:103-122, 319-329) and
+ * PoissonLogLikelihood.compute_gradient (likelihoods/poisson_log_likelihood.py:16-36).
+ * predicted (optional, device [n_sel][ny][nz]) receives H_m f + s_m. */
+gb_status gb_spect_osem_step(gb_spect_plan *plan, float *object, const float *projections,
+                             const float *additive, const float *norm_bp, int32_t subset,
+                             float *predicted, gb_stream_t stream);
+
+/* Relative-difference prior with Euclidean neighbour weights
+ * (priors/nearest_neighbour.py:156-183, 207-220). */
+typedef struct gb_rdp_desc {
+    float beta, gamma, delta;  /* delta: pytomography.delta at prior construction */
+    const float *fov_scale;    /* device [nx][ny][nz] or NULL (all ones) */
+} gb_rdp_desc;
+
+/* One fused BSREM sub-iteration (PGA:436-474):
+ *   out = in + in * relax / (w_m * sum_k normBP_k + delta)
+ *              * (H_m^T (g_m/(H_m in + s_m + delta)) - normBP_m - grad V(in) * w_m),
+ *   out[out <= floor] = floor,
+ * grad V from the RDP prior (prior may be NULL: no prior).  in and out must differ. */
+gb_status gb_spect_bsrem_step(gb_spect_plan *plan, const float *object_in, float *object_out,
+                              const float *projections, const float *additive,
+                              const float *norm_bp, const float *norm_bp_sum, float relax,
+                              float subset_weight, const gb_rdp_desc *prior, float floor_value,
+                              int32_t subset, gb_stream_t stream);
+
+/* RDP gradient beta * scale * sum_s w_rs phi1(f_r, f_s) * fov_scale
+ * (nearest_neighbour.py:44-75 with phi1 of :176-177), replicate boundary. */
+gb_status gb_rdp_gradient(const float *object, float *grad, int32_t nx, int32_t ny,
+                          int32_t nz, float dx, float dy, float dz, const gb_rdp_desc *prior,
+                          float beta_scale, gb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBTOMO_H */

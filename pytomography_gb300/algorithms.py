@@ -1,0 +1,182 @@
+"""OSEM / BSREM update loop.
+
+Mirror of ``PreconditionedGradientAscentAlgorithm.__call__``, ``OSEM`` and ``BSREM``
+(src/pytomography/algorithms/preconditioned_gradient_ascent.py:14-129, 301-329, 436-474).
+
+Two execution forms share the loop:
+
+* ``fused=True`` (default when the system matrix is this package's
+  ``SPECTSystemMatrix`` and the likelihood is ``PoissonLogLikelihood``): each
+  sub-iteration is one C-ABI call (``gb_spect_osem_step`` / ``gb_spect_bsrem_step``):
+  forward kernel with the g/(Hf+s+delta) epilogue, back-projection kernels, and the
+  preconditioned update (and, for BSREM, the RDP gradient) fused into the last one.
+* ``fused=False``: the reference's own sequence of forward, torch elementwise ratio,
+  backward and torch elementwise update ("plain" per-call path).
+"""
+from __future__ import annotations
+
+from collections.abc import Callable
+
+import torch
+
+import pytomography_gb300 as _p
+
+from .likelihoods import PoissonLogLikelihood
+
+
+class PreconditionedGradientAscentAlgorithm:
+    def __init__(self, likelihood, prior=None, object_initial: torch.Tensor | None = None,
+                 addition_after_iteration: float = 0, fused: bool | None = None, **kwargs) -> None:
+        self.likelihood = likelihood
+        if object_initial is None:
+            self.object_prediction = likelihood.system_matrix._get_object_initial(_p.device)
+        else:
+            self.object_prediction = object_initial.to(_p.device).to(_p.dtype)
+        self.prior = prior
+        if self.prior is not None:
+            self.prior.set_object_meta(likelihood.system_matrix.object_meta)
+            self.prior.set_FOV_scale(likelihood.system_matrix._get_prior_FOV_scale())
+        self.objects_stored = []
+        self.projections_predicted_stored = []
+        self.addition_after_iteration = addition_after_iteration
+        self._fused_request = fused
+
+    def _set_n_subsets(self, n_subsets: int) -> None:
+        self.n_subsets = n_subsets
+        self.likelihood._set_n_subsets(n_subsets)
+
+    def _compute_preconditioner(self, object, n_iter, n_subset):
+        raise NotImplementedError
+
+    def _compute_callback(self, n_iter: int, n_subset: int) -> None:
+        self.object_prediction = self.callback.run(self.object_prediction, n_iter, n_subset)
+
+    def _can_fuse(self) -> bool:
+        from .projectors.SPECT import SPECTSystemMatrix
+        ok = (isinstance(self.likelihood.system_matrix, SPECTSystemMatrix)
+              and type(self.likelihood) is PoissonLogLikelihood and self._fused_kind() is not None)
+        if self._fused_request is True and not ok:
+            raise NotImplementedError("this likelihood / system matrix / prior has no fused step")
+        return ok if self._fused_request is None else bool(self._fused_request)
+
+    def _fused_kind(self):
+        return None
+
+    def _fused_begin(self) -> None:
+        pass
+
+    def _fused_step(self, j: int, subset_idx):
+        raise NotImplementedError
+
+    def __call__(self, n_iters: int, n_subsets: int = 1, n_subset_specific: int | None = None,
+                 callback=None):
+        self.callback = callback
+        self.n_iters = n_iters
+        self._set_n_subsets(n_subsets)
+        fused = self._can_fuse()
+        if fused:
+            self.object_prediction = self.object_prediction.to(torch.float32).contiguous()
+            self._fused_begin()
+        for j in range(n_iters):
+            for k in range(n_subsets):
+                if n_subset_specific is not None and n_subset_specific != k:
+                    continue
+                subset_idx = None if n_subsets == 1 else k
+                if fused:
+                    self._fused_step(j, subset_idx)
+                else:
+                    if bool(self.prior):
+                        self.prior.set_object(torch.clone(self.object_prediction).to(_p.device))
+                        self.prior.set_beta_scale(
+                            self.likelihood.system_matrix.get_weighting_subset(subset_idx))
+                        self.prior_gradient = self.prior(derivative_order=1)
+                    else:
+                        self.prior_gradient = 0
+                    grad = self.likelihood.compute_gradient(self.object_prediction, subset_idx)
+                    pre = self._compute_preconditioner(self.object_prediction, j, subset_idx)
+                    self.object_prediction += pre * (grad - self.prior_gradient)
+                    self.object_prediction[self.object_prediction <= self.addition_after_iteration] = \
+                        self.addition_after_iteration
+                if self.callback is not None:
+                    self._compute_callback(n_iter=j, n_subset=k)
+        if self.callback is not None:
+            self.callback.finalize(self.object_prediction)
+        return self.object_prediction
+
+
+class LinearPreconditionedGradientAscentAlgorithm(PreconditionedGradientAscentAlgorithm):
+    def _linear_preconditioner_factor(self, n_iter: int, n_subset: int):
+        raise NotImplementedError
+
+    def _compute_preconditioner(self, object, n_iter, n_subset):
+        return object * self._linear_preconditioner_factor(n_iter, n_subset)
+
+
+class OSEM(LinearPreconditionedGradientAscentAlgorithm):
+    """f <- f + f / H_m^T 1 * grad L."""
+
+    def __init__(self, likelihood, object_initial: torch.Tensor | None = None,
+                 fused: bool | None = None) -> None:
+        super().__init__(likelihood=likelihood, object_initial=object_initial, fused=fused)
+
+    def _linear_preconditioner_factor(self, n_iter, n_subset):
+        return 1 / (self.likelihood._get_normBP(n_subset) + _p.delta)
+
+    def _fused_kind(self):
+        return "osem"
+
+    def _fused_step(self, j, subset_idx):
+        lik = self.likelihood
+        sm = lik.system_matrix
+        n_sel = sm._n_sel(subset_idx)
+        pred = getattr(self, "_pred_buf", None)
+        if pred is None or pred.shape[0] != n_sel:
+            pred = torch.empty((n_sel, *sm.proj_meta.shape[1:]), device=sm.device)
+            self._pred_buf = pred
+        s = lik.additive_term if lik.exists_additive_term else None
+        sm.osem_step(self.object_prediction, lik.projections, s, lik._get_normBP(subset_idx),
+                     subset_idx, predicted=pred)
+        lik.projections_predicted = pred
+
+
+class BSREM(LinearPreconditionedGradientAscentAlgorithm):
+    """f <- f + alpha(n) f / (w_m sum_k H_k^T 1) * (grad L - grad V), floor 1e-4."""
+
+    def __init__(self, likelihood, object_initial: torch.Tensor | None = None, prior=None,
+                 relaxation_sequence: Callable = lambda _: 1, addition_after_iteration=1e-4,
+                 fused: bool | None = None) -> None:
+        self.relaxation_sequence = relaxation_sequence
+        super().__init__(likelihood=likelihood, object_initial=object_initial, prior=prior,
+                         addition_after_iteration=addition_after_iteration, fused=fused)
+
+    def _linear_preconditioner_factor(self, n_iter, n_subset):
+        relaxation_factor = self.relaxation_sequence(n_iter)
+        norm_BP = self.likelihood._get_normBP(n_subset, return_sum=True)
+        w = self.likelihood.system_matrix.get_weighting_subset(n_subset)
+        return relaxation_factor / (w * norm_BP + _p.delta)
+
+    def _fused_kind(self):
+        from .priors import RelativeDifferencePrior
+        if self.prior is None or isinstance(self.prior, RelativeDifferencePrior):
+            return "bsrem"
+        return None
+
+    def _fused_begin(self) -> None:
+        lik = self.likelihood
+        self._nbp_sum = lik._get_normBP(None if self.n_subsets == 1 else 0,
+                                        return_sum=True).contiguous()
+
+    def _fused_step(self, j, subset_idx):
+        lik = self.likelihood
+        sm = lik.system_matrix
+        out = getattr(self, "_pingpong", None)
+        if out is None or out.shape != self.object_prediction.shape:
+            out = torch.empty_like(self.object_prediction)
+        s = lik.additive_term if lik.exists_additive_term else None
+        sm.bsrem_step(self.object_prediction, out, lik.projections, s,
+                      lik._get_normBP(subset_idx).contiguous(), self._nbp_sum,
+                      float(self.relaxation_sequence(j)), float(sm.get_weighting_subset(subset_idx)),
+                      prior=self.prior, floor_value=float(self.addition_after_iteration),
+                      subset_idx=subset_idx)
+        self._pingpong = self.object_prediction
+        self.object_prediction = out

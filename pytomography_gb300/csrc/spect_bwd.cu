@@ -1,0 +1,398 @@
+// SPECT back-projectors, attenuation precompute, OSEM/BSREM update epilogues and the
+// relative-difference prior.
+//
+// Reference back-projector: SPECTSystemMatrix.backward
+// (projectors/SPECT/spect_system_matrix.py:159-201): the projection row is broadcast
+// along x inside the back-projection box (utils/spatial.py:75-79), the obj2obj
+// transforms are applied in reverse order (PSF: psf.py:216-231, attenuation:
+// attenuation.py:94-115), and the result is rotated back by +(270 - beta) with bilinear
+// interpolation (transforms/shared/spatial.py:21-36) and summed.
+//
+// Two kernels per angle group:
+//   k_b1_psf / k_b1_nopsf : rotated frame, W[xp][y][z] = A (.) PSF_xp(P) (or PSF(A (.) P))
+//   k_b2_gather           : object frame, bilinear gather of W at the back-rotation
+//                           (reference operator), fused OSEM / BSREM update epilogue
+//   k_b2_scatter          : exact transpose of the forward's gather (adjoint operator)
+#include "spect_kernels.cuh"
+#include "spect_launch.h"
+
+namespace gb {
+
+// ------------------------------------------------------------- attenuation
+// A[a][xp][y][z] = exp(-(sum_{k>=xp} mu_rot[k]*dx - mu_rot[xp]*dx/2)) for the stored
+// rows y in [ya_lo, ya_hi); mu_rot uses the forward rotation of angle a.
+// (get_prob_of_detection_matrix, attenuation.py:11-21; rev_cumsum, utils/misc.py:8-19)
+__global__ void k_atten(SpectDev g, const float *__restrict__ mu, float dx, float *__restrict__ A) {
+    const int a = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nya * g.nz) return;
+    const int r = i / g.nz, z = i % g.nz;
+    const int y = g.ya_lo + r;
+    float th[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * a + k];
+    const float lc = g.lin[y];
+    float *out = A + (size_t)a * g.Lp * g.nya * g.nz + (size_t)r * g.nz + z;
+    const size_t plane = (size_t)g.nya * g.nz;
+    float run = 0.f;
+    for (int xp = g.Lp - 1; xp >= 0; --xp) {
+        float ix, iy;
+        rot_coords(th, g.lin[xp], lc, g.half, ix, iy);
+        Bilin b = bilin(ix, iy);
+        float v = __fmul_rn(sample(mu, g.N, g.N, g.nz, g.pad, g.pad, b, z), dx);
+        run = __fadd_rn(run, v);
+        out[(size_t)xp * plane] = expf(-__fsub_rn(run, __fmul_rn(v, 0.5f)));
+    }
+}
+
+cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_angles, float *A,
+                         cudaStream_t st) {
+    dim3 grid((g.nya * g.nz + 255) / 256, n_angles);
+    k_atten<<<grid, 256, 0, st>>>(g, mu, dx, A);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- B1 (PSF)
+// Grid (chunk of planes, angle slot, z slab).  Output rows o <-> padded y = pad-H+o,
+// o in [0, N+2H); input S rows i <-> padded y = pad-2H+i (projection rows at i in
+// [2H, 2H+N), zero elsewhere).
+template <int K>
+__global__ void __launch_bounds__(512, 1)
+    k_b1_psf(SpectDev g, const float *__restrict__ proj, const int *__restrict__ alist,
+             int n_chunks, int Zt, float *__restrict__ W) {
+    constexpr int H = K / 2;
+    constexpr int OB = (K <= 31) ? 8 : 4;
+    const int slot = blockIdx.y, chunk = blockIdx.x;
+    const int ga = alist[slot];
+    const int N = g.N, nz = g.nz;
+    const int z0 = blockIdx.z * Zt;
+    const int Zc = min(Zt, nz - z0);
+    const int NO = N + 2 * H;                       // output rows
+    const int O8 = (NO + OB - 1) / OB * OB;
+    const int Z8 = (Zc + OB - 1) / OB * OB;
+    const int SC = Z8 + 2 * H, SR = O8 + 2 * H;     // S: [SR][SC]
+    const int TS = O8 + 1, TR = Z8 + 2 * H;         // Tt: [TR][TS]
+    extern __shared__ float sm[];
+    float *S = sm;
+    float *Tt = S + SR * SC;
+    float *tp = Tt + TR * TS;
+    for (int i = threadIdx.x; i < SR * SC + TR * TS; i += blockDim.x) sm[i] = 0.f;
+    const int grp = g.group[ga];
+    const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
+    const int x0 = chunk * g.Lp / n_chunks, x1 = (chunk + 1) * g.Lp / n_chunks;
+    const int cz_lo = max(0, H - z0), cz_hi = min(SC, nz - z0 + H);
+    const int ncol = cz_hi - cz_lo;
+    const float *P = proj + (size_t)slot * N * nz;
+    const bool att_inside = A && !g.att_first;  // "pa": A multiplies before the blur
+    __syncthreads();
+    if (!att_inside) {
+        for (int i = threadIdx.x; i < N * ncol; i += blockDim.x) {
+            int y = i / ncol, c = cz_lo + i % ncol;
+            S[(2 * H + y) * SC + c] = P[(size_t)y * nz + (z0 - H + c)];
+        }
+    }
+    const int n3 = O8 * (Z8 / OB);
+    int parity = 0;
+    for (int xp = x0; xp < x1; ++xp) {
+        float *tap = tp + parity * 2 * K;
+        if (threadIdx.x < K) {
+            tap[threadIdx.x] = g.taps_r[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x];
+            tap[K + threadIdx.x] =
+                g.psf2d ? g.taps_z[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x] : 0.f;
+        }
+        const float *Ap = A ? A + (size_t)xp * g.nya * nz : nullptr;
+        if (att_inside) {
+            for (int i = threadIdx.x; i < N * ncol; i += blockDim.x) {
+                int y = i / ncol, c = cz_lo + i % ncol;
+                int z = z0 - H + c;
+                S[(2 * H + y) * SC + c] = __fmul_rn(
+                    P[(size_t)y * nz + z], Ap[(size_t)(g.pad + y - g.ya_lo) * nz + z]);
+            }
+        }
+        __syncthreads();
+        {
+            float w[K];
+#pragma unroll
+            for (int t = 0; t < K; t++) w[t] = tap[t];
+            for (int task = threadIdx.x; task < ncol * (O8 / OB); task += blockDim.x) {
+                int c = cz_lo + task % ncol, ob = task / ncol;
+                float win[OB + K - 1];
+#pragma unroll
+                for (int i = 0; i < OB + K - 1; i++) win[i] = S[(ob * OB + i) * SC + c];
+#pragma unroll
+                for (int j = 0; j < OB; j++) {
+                    float o = 0.f;
+#pragma unroll
+                    for (int t = 0; t < K; t++) o = fmaf(w[t], win[j + t], o);
+                    Tt[c * TS + ob * OB + j] = o;
+                }
+            }
+        }
+        __syncthreads();
+        {
+            float w[K];
+#pragma unroll
+            for (int t = 0; t < K; t++) w[t] = tap[K + t];
+            float *Wp = W + ((size_t)slot * g.Lp + xp) * g.nya * nz;
+            for (int task = threadIdx.x; task < n3; task += blockDim.x) {
+                int o_row = task % O8, zb = task / O8;
+                int y = g.pad - H + o_row;
+                float o[OB];
+                if (g.psf2d) {
+                    float win[OB + K - 1];
+#pragma unroll
+                    for (int i = 0; i < OB + K - 1; i++) win[i] = Tt[(zb * OB + i) * TS + o_row];
+#pragma unroll
+                    for (int j = 0; j < OB; j++) {
+                        float s = 0.f;
+#pragma unroll
+                        for (int t = 0; t < K; t++) s = fmaf(w[t], win[j + t], s);
+                        o[j] = s;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + H) * TS + o_row];
+                }
+                if (o_row >= NO || y < g.ya_lo || y >= g.ya_hi) continue;
+#pragma unroll
+                for (int j = 0; j < OB; j++) {
+                    int zl = zb * OB + j;
+                    if (zl >= Zc) continue;
+                    int z = z0 + zl;
+                    float v = o[j];
+                    if (Ap && g.att_first) v = __fmul_rn(v, Ap[(size_t)(y - g.ya_lo) * nz + z]);
+                    Wp[(size_t)(y - g.ya_lo) * nz + z] = v;
+                }
+            }
+        }
+        parity ^= 1;
+    }
+}
+
+// -------------------------------------------------------------- B1 (no PSF)
+// W[slot][xp][y][z] = P[y - pad][z] * A (rows [pad, pad+N) are the stored rows).
+__global__ void k_b1_nopsf(SpectDev g, const float *__restrict__ proj,
+                           const int *__restrict__ alist, float *__restrict__ W) {
+    const int slot = blockIdx.z, xp = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nya * g.nz) return;
+    const int r = i / g.nz, z = i % g.nz;
+    const int y = g.ya_lo + r;
+    const int ga = alist[slot];
+    float v = 0.f;
+    if (y >= g.pad && y < g.pad + g.N) {
+        v = proj[((size_t)slot * g.N + (y - g.pad)) * g.nz + z];
+        if (g.att)
+            v = __fmul_rn(v, __ldg(g.A + (((size_t)ga * g.Lp + xp) * g.nya + r) * g.nz + z));
+    }
+    W[(((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z] = v;
+}
+
+template <int K>
+static cudaError_t launch_b1_psf_k(const SpectDev &g, const float *proj, const int *alist,
+                                   int n_slots, int n_chunks, int Zt, float *W, cudaStream_t st) {
+    size_t smem = b1_psf_smem_bytes(K, g.N, Zt);
+    dim3 grid(n_chunks, n_slots, (g.nz + Zt - 1) / Zt);
+    k_b1_psf<K><<<grid, 512, smem, st>>>(g, proj, alist, n_chunks, Zt, W);
+    return cudaGetLastError();
+}
+
+template <int K>
+static cudaError_t setup_b1_k(size_t smem) {
+    return cudaFuncSetAttribute(k_b1_psf<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
+}
+
+cudaError_t setup_b1(int K, size_t smem) {
+    switch (K) {
+#define GB_SETUP_CASE(KK) \
+    case KK:              \
+        return setup_b1_k<KK>(smem);
+        GB_FOR_EACH_K(GB_SETUP_CASE)
+#undef GB_SETUP_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+size_t b1_psf_smem_bytes(int K, int N, int Zt) {
+    int H = K / 2, OB = (K <= 31) ? 8 : 4;
+    int O8 = (N + 2 * H + OB - 1) / OB * OB;
+    int Z8 = (Zt + OB - 1) / OB * OB;
+    return sizeof(float) *
+           ((size_t)(O8 + 2 * H) * (Z8 + 2 * H) + (size_t)(Z8 + 2 * H) * (O8 + 1) + 4 * K);
+}
+
+cudaError_t launch_b1(const SpectDev &g, const float *proj, const int *alist, int n_slots,
+                      int n_chunks, int Zt, float *W, cudaStream_t st) {
+    if (!g.psf) {
+        dim3 grid((g.nya * g.nz + 255) / 256, g.Lp, n_slots);
+        k_b1_nopsf<<<grid, 256, 0, st>>>(g, proj, alist, W);
+        return cudaGetLastError();
+    }
+    switch (g.K) {
+#define GB_B1_CASE(KK) \
+    case KK:           \
+        return launch_b1_psf_k<KK>(g, proj, alist, n_slots, n_chunks, Zt, W, st);
+        GB_FOR_EACH_K(GB_B1_CASE)
+#undef GB_B1_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+// ------------------------------------------------------------- RDP helpers
+// sum_s w_rs phi1(f_r, f_s) over the 26 neighbours with replicate boundary, in the
+// loop order of NearestNeighbourPrior._pair_contribution (nearest_neighbour.py:56-72);
+// phi1 of RelativeDifferencePrior (nearest_neighbour.py:176-177).
+__device__ __forceinline__ float rdp_sum(const float *__restrict__ f, int nx, int ny, int nz,
+                                         int x, int y, int z, float fr, const UpdateArgs &u) {
+    float acc = 0.f;
+    int n = 0;
+    const float two_d = 2.f * u.rdelta;
+#pragma unroll
+    for (int i = -1; i <= 1; i++) {
+        int xi = min(max(x + i, 0), nx - 1);
+#pragma unroll
+        for (int j = -1; j <= 1; j++) {
+            int yj = min(max(y + j, 0), ny - 1);
+#pragma unroll
+            for (int k = -1; k <= 1; k++) {
+                if (i == 0 && j == 0 && k == 0) continue;
+                int zk = min(max(z + k, 0), nz - 1);
+                float fs = __ldg(f + ((size_t)xi * ny + yj) * nz + zk);
+                float d = __fsub_rn(fr, fs);
+                float ad = fabsf(d);
+                float num = __fmul_rn(
+                    d, __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(u.gamma, ad), __fmul_rn(3.f, fs)), fr),
+                                 two_d));
+                float den = __fadd_rn(__fadd_rn(__fadd_rn(fr, fs), __fmul_rn(u.gamma, ad)), u.rdelta);
+                float phi = __fdiv_rn(num, __fmul_rn(den, den));
+                acc = __fadd_rn(acc, __fmul_rn(phi, u.w26[n]));
+                n++;
+            }
+        }
+    }
+    return acc;
+}
+
+__global__ void k_rdp(const float *__restrict__ f, float *__restrict__ grad, int nx, int ny,
+                      int nz, UpdateArgs u, float scale) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)nx * ny * nz) return;
+    int z = i % nz, y = (i / nz) % ny, x = i / ((size_t)nz * ny);
+    float s = rdp_sum(f, nx, ny, nz, x, y, z, f[i], u);
+    float v = __fmul_rn(scale, s);
+    if (u.fov) v = __fmul_rn(v, u.fov[i]);
+    grad[i] = v;
+}
+
+cudaError_t launch_rdp(const float *f, float *grad, int nx, int ny, int nz, const UpdateArgs &u,
+                       float beta_scale, cudaStream_t st) {
+    size_t n = (size_t)nx * ny * nz;
+    k_rdp<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(f, grad, nx, ny, nz, u,
+                                                      u.beta * beta_scale);
+    return cudaGetLastError();
+}
+
+// Update epilogue shared by the gather kernel and the standalone update kernel.
+__device__ __forceinline__ void apply_update(int mode, const UpdateArgs &u, size_t i, int x,
+                                             int y, int z, int nx, int ny, int nz, float bp,
+                                             float *out) {
+    if (u.acc) bp = __fadd_rn(u.acc[i], bp);
+    if (mode == B2_WRITE) {
+        out[i] = bp;
+    } else if (mode == B2_ADD) {
+        out[i] = __fadd_rn(out[i], bp);
+    } else if (mode == B2_OSEM) {
+        float f = u.f[i], nb = u.nbp[i];
+        float grad = __fsub_rn(bp, nb);
+        float pre = __fmul_rn(f, __frcp_rn(__fadd_rn(nb, kDelta)));
+        float fn = __fadd_rn(f, __fmul_rn(pre, grad));
+        u.f[i] = fn <= 0.f ? 0.f : fn;
+    } else {  // B2_BSREM
+        float f = u.f_in[i], nb = u.nbp[i];
+        float grad = __fsub_rn(bp, nb);
+        if (u.prior) {
+            float v = __fmul_rn(__fmul_rn(u.beta, u.w_m),
+                                rdp_sum(u.f_in, nx, ny, nz, x, y, z, f, u));
+            if (u.fov) v = __fmul_rn(v, u.fov[i]);
+            grad = __fsub_rn(grad, v);
+        }
+        float pre = __fmul_rn(
+            f, __fdiv_rn(u.relax, __fadd_rn(__fmul_rn(u.w_m, u.nbp_sum[i]), kDelta)));
+        float fn = __fadd_rn(f, __fmul_rn(pre, grad));
+        u.f_out[i] = fn <= u.floor_v ? u.floor_v : fn;
+    }
+}
+
+// ------------------------------------------------------------- B2 gather
+// Reference back-projector: for every object voxel, bilinear sample of W at the
+// back-rotation (angle 270 - beta) of each angle of the group, summed.
+__global__ void __launch_bounds__(256)
+    k_b2_gather(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
+                int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
+    const int z = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 8 + threadIdx.y;
+    const int x = blockIdx.z;
+    const int N = g.N, nz = g.nz;
+    if (z >= nz || y >= N) return;
+    const float lr = g.lin[x + g.pad], lc = g.lin[y + g.pad];
+    const size_t slab = (size_t)g.Lp * g.nya * nz;
+    float bp = 0.f;
+    for (int s = 0; s < n_slots; s++) {
+        const float *th = g.theta_bwd + 6 * alist[s];
+        float ix, iy;
+        rot_coords(th, lr, lc, g.half, ix, iy);
+        Bilin b = bilin(ix, iy);
+        // W rows = padded x (row offset 0), cols = padded y - ya_lo
+        bp = __fadd_rn(bp, sample(W + s * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b, z));
+    }
+    const size_t i = ((size_t)x * N + y) * nz + z;
+    apply_update(mode, u, i, x, y, z, N, N, nz, bp, out);
+}
+
+cudaError_t launch_b2_gather(const SpectDev &g, const float *W, const int *alist, int n_slots,
+                             float *out, int mode, const UpdateArgs &u, cudaStream_t st) {
+    dim3 block(32, 8);
+    dim3 grid((g.nz + 31) / 32, (g.N + 7) / 8, g.N);
+    k_b2_gather<<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ B2 scatter
+// Exact adjoint of the forward rotation: every W element is scattered to the four
+// object voxels the forward sample at the same position gathered from.
+__global__ void __launch_bounds__(256)
+    k_b2_scatter(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
+                 float *__restrict__ out) {
+    const int slot = blockIdx.z, xp = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nya * g.nz) return;
+    const int r = i / g.nz, z = i % g.nz;
+    const int yp = g.ya_lo + r;
+    const float v = W[(((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z];
+    if (v == 0.f) return;
+    const float *th = g.theta_fwd + 6 * alist[slot];
+    float ix, iy;
+    rot_coords(th, g.lin[xp], g.lin[yp], g.half, ix, iy);
+    Bilin b = bilin(ix, iy);
+    const int N = g.N, nz = g.nz;
+    const int r0 = b.r0 - g.pad, c0 = b.c0 - g.pad;
+    const float wt[4] = {b.nw, b.ne, b.sw, b.se};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        int rr = r0 + (q >> 1), cc = c0 + (q & 1);
+        if ((unsigned)rr < (unsigned)N && (unsigned)cc < (unsigned)N)
+            atomicAdd(out + ((size_t)rr * N + cc) * nz + z, __fmul_rn(wt[q], v));
+    }
+}
+
+cudaError_t launch_b2_scatter(const SpectDev &g, const float *W, const int *alist, int n_slots,
+                              float *out, cudaStream_t st) {
+    dim3 grid((g.nya * g.nz + 255) / 256, g.Lp, n_slots);
+    k_b2_scatter<<<grid, 256, 0, st>>>(g, W, alist, out);
+    return cudaGetLastError();
+}
+
+}  // namespace gb

@@ -1,0 +1,117 @@
+// SPECT rotate+sum kernels for sm_103a (GB300).
+//
+// Frames and layouts
+//   object f      [N][N][nz]   unpadded, z fastest
+//   padded frame  Lp = N + 2*pad rows (x) and cols (y); f_pad[r][c] = f[r-pad][c-pad]
+//   projections   [n_sel][N][nz]
+//   A (attenuation factors, per angle, rotated padded frame)  [n_angles][Lp][nya][nz],
+//                 rows y in [ya_lo, ya_hi) only (the rows the PSF halo can reach)
+//   W (back-projection stack of one angle group)              [G][Lp][nya][nz]
+//
+// Rotation convention (kornia, align_corners=True; utils/spatial.py:8-34,
+// transforms/shared/spatial.py:21-53): an output voxel (row xp, col yp) samples
+//   col = (th0*lin[yp] + th1*lin[xp] + th2 + 1) * (Lp-1)/2
+//   row = (th3*lin[yp] + th4*lin[xp] + th5 + 1) * (Lp-1)/2
+// bilinearly with zero padding; the arithmetic below keeps the operation order of
+// the grid_sample CPU kernel (no FMA contraction) so the taps are reproducible.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gb {
+
+constexpr float kDelta = 1e-11f;  // pytomography.delta (src/pytomography/__init__.py:21)
+
+struct SpectDev {
+    int N, nz, pad, Lp;
+    int ya_lo, ya_hi, nya;  // stored row range of A and W
+    float half;             // (Lp - 1) / 2
+    const float *lin;       // [Lp]
+    const float *theta_fwd; // [n_angles][6]
+    const float *theta_bwd; // [n_angles][6]
+    const float *A;         // [n_angles][Lp][nya][nz] or null
+    const float *taps_r;    // [n_groups][Lp][K]
+    const float *taps_z;    // [n_groups][Lp][K]
+    const int *group;       // [n_angles]
+    int K;                  // taps per row (odd)
+    int att;                // attenuation present
+    int att_first;          // forward order: attenuation before PSF ("ap")
+    int psf;                // PSF present
+    int psf2d;              // PSF blurs z as well
+};
+
+// Epilogue of the gather back-projector.
+enum B2Mode : int {
+    B2_WRITE = 0,   // out = bp
+    B2_ADD = 1,     // out += bp
+    B2_OSEM = 2,    // f += f/(nbp+d) * ((bp + acc) - nbp); clamp <= 0 -> 0
+    B2_BSREM = 3,   // out = in + in*relax/(w*nbp_sum+d) * ((bp+acc) - nbp - rdp); clamp floor
+};
+
+struct UpdateArgs {
+    float *f;              // OSEM: object updated in place
+    const float *nbp;      // H_m^T 1
+    const float *acc;      // partial back projection of earlier angle groups (or null)
+    const float *f_in;     // BSREM input object
+    float *f_out;          // BSREM output object
+    const float *nbp_sum;  // BSREM: sum_k H_k^T 1
+    float relax, w_m;      // BSREM relaxation and subset weight
+    int prior;             // BSREM: RDP present
+    float beta, gamma, rdelta;
+    const float *fov;      // RDP FOV scale or null
+    float w26[26];         // RDP neighbour weights, loop order i,j,k in {-1,0,1}
+    float floor_v;         // BSREM clamp value
+};
+
+__device__ __forceinline__ void rot_coords(const float *__restrict__ th, float lin_row,
+                                           float lin_col, float half, float &ix, float &iy) {
+    float gx = __fadd_rn(__fadd_rn(__fmul_rn(th[0], lin_col), __fmul_rn(th[1], lin_row)), th[2]);
+    float gy = __fadd_rn(__fadd_rn(__fmul_rn(th[3], lin_col), __fmul_rn(th[4], lin_row)), th[5]);
+    ix = __fmul_rn(__fadd_rn(gx, 1.f), half);
+    iy = __fmul_rn(__fadd_rn(gy, 1.f), half);
+}
+
+struct Bilin {
+    int r0, c0;
+    float nw, ne, sw, se;
+};
+
+__device__ __forceinline__ Bilin bilin(float ix, float iy) {
+    Bilin b;
+    float fx = floorf(ix), fy = floorf(iy);
+    float w = __fsub_rn(ix, fx), e = __fsub_rn(1.f, w);
+    float n = __fsub_rn(iy, fy), s = __fsub_rn(1.f, n);
+    b.c0 = (int)fx;
+    b.r0 = (int)fy;
+    b.nw = __fmul_rn(s, e);
+    b.ne = __fmul_rn(s, w);
+    b.sw = __fmul_rn(n, e);
+    b.se = __fmul_rn(n, w);
+    return b;
+}
+
+__device__ __forceinline__ float bilin_combine(const Bilin &b, float vnw, float vne, float vsw,
+                                               float vse) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(vnw, b.nw), __fmul_rn(vne, b.ne)),
+                               __fmul_rn(vsw, b.sw)),
+                     __fmul_rn(vse, b.se));
+}
+
+// Bilinear sample of a [rows][cols][nz] array whose (row, col) origin is shifted by
+// (row_off, col_off): value at (r, c) = src[r - row_off][c - col_off] when inside.
+__device__ __forceinline__ float sample(const float *__restrict__ src, int rows, int cols,
+                                        int nz, int row_off, int col_off, const Bilin &b,
+                                        int z) {
+    int r = b.r0 - row_off, c = b.c0 - col_off;
+    bool r0 = (unsigned)r < (unsigned)rows, r1 = (unsigned)(r + 1) < (unsigned)rows;
+    bool c0 = (unsigned)c < (unsigned)cols, c1 = (unsigned)(c + 1) < (unsigned)cols;
+    if (!((r0 || r1) && (c0 || c1))) return 0.f;
+    const float *p = src + ((long long)r * cols + c) * nz + z;
+    float vnw = (r0 && c0) ? __ldg(p) : 0.f;
+    float vne = (r0 && c1) ? __ldg(p + nz) : 0.f;
+    float vsw = (r1 && c0) ? __ldg(p + (long long)cols * nz) : 0.f;
+    float vse = (r1 && c1) ? __ldg(p + (long long)cols * nz + nz) : 0.f;
+    return bilin_combine(b, vnw, vne, vsw, vse);
+}
+
+}  // namespace gb

@@ -1,0 +1,43 @@
+// Host-side launchers of the SPECT kernels (implemented in spect_fwd.cu / spect_bwd.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "spect_kernels.cuh"
+
+// PSF tap-count buckets compiled into the library: a plan's taps are zero-padded
+// (centred) to the smallest bucket that holds its widest kernel.
+#define GB_FOR_EACH_K(X) X(7) X(11) X(15) X(21) X(25) X(29) X(37) X(45)
+
+namespace gb {
+
+inline int psf_bucket(int k) {
+    const int b[] = {7, 11, 15, 21, 25, 29, 37, 45};
+    for (int v : b)
+        if (k <= v) return v;
+    return -1;
+}
+
+size_t fwd_psf_smem_bytes(int K, int N, int Zt);
+size_t b1_psf_smem_bytes(int K, int N, int Zt);
+// Raise the dynamic shared-memory limit of the PSF kernels (done once at plan creation,
+// outside any stream capture).
+cudaError_t setup_fwd(int K, size_t smem);
+cudaError_t setup_b1(int K, size_t smem);
+
+cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, int n_slots,
+                       int n_chunks, int Zt, float *partials, cudaStream_t st);
+cudaError_t launch_reduce(int n_slots, int n_chunks, int NZ, const float *partials, float *out,
+                          int ratio, const float *gproj, const float *sadd, const int *alist,
+                          float *pred, cudaStream_t st);
+cudaError_t launch_b1(const SpectDev &g, const float *proj, const int *alist, int n_slots,
+                      int n_chunks, int Zt, float *W, cudaStream_t st);
+cudaError_t launch_b2_gather(const SpectDev &g, const float *W, const int *alist, int n_slots,
+                             float *out, int mode, const UpdateArgs &u, cudaStream_t st);
+cudaError_t launch_b2_scatter(const SpectDev &g, const float *W, const int *alist, int n_slots,
+                              float *out, cudaStream_t st);
+cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_angles, float *A,
+                         cudaStream_t st);
+cudaError_t launch_rdp(const float *f, float *grad, int nx, int ny, int nz, const UpdateArgs &u,
+                       float beta_scale, cudaStream_t st);
+
+}  // namespace gb

@@ -1,0 +1,269 @@
+"""Drop-in ``SPECTSystemMatrix`` running the fused sm_103a projector.
+
+Mirror of src/pytomography/projectors/SPECT/spect_system_matrix.py:15-201.  The
+constructor takes the reference's arguments; the obj2obj plugins
+(``SPECTAttenuationTransform``, ``SPECTPSFTransform``) are lowered into one CUDA plan
+(geometry tables, attenuation factors per angle, per-plane PSF taps) and every projection
+is a few kernel launches through ``libgbtomo.so``.  Unknown transforms raise; there is no
+CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib, geometry
+from ..transforms.SPECT import SPECTAttenuationTransform, SPECTPSFTransform
+from .system_matrix import SystemMatrix
+
+
+class SPECTSystemMatrix(SystemMatrix):
+    """Rotate+sum SPECT system matrix.
+
+    Args:
+        obj2obj_transforms: attenuation and/or PSF plugins, in application order.
+        proj2proj_transforms: must be empty (no proj2proj plugin is on this path).
+        object_meta, proj_meta: SPECT metadata.
+        object_initial_based_on_camera_path: zero voxels the camera path never sees.
+        psf_trunc_rel: PSF taps below this fraction of a plane's largest tap are skipped
+            (0 keeps the reference's full kernel).
+    """
+
+    def __init__(self, obj2obj_transforms, proj2proj_transforms, object_meta, proj_meta,
+                 object_initial_based_on_camera_path: bool = False,
+                 psf_trunc_rel: float = 0.0) -> None:
+        if proj2proj_transforms:
+            raise NotImplementedError("proj2proj transforms are not part of the fused path")
+        super().__init__(object_meta, proj_meta, obj2obj_transforms, proj2proj_transforms)
+        self.object_initial_based_on_camera_path = object_initial_based_on_camera_path
+        self.psf_trunc_rel = float(psf_trunc_rel)
+        self._plan = None
+        self._lib = _lib.load()
+        self._build_plan()
+        self.subset_indices_array = None
+        self.n_subsets = 1
+
+    # ------------------------------------------------------------ plan
+    def _build_plan(self) -> None:
+        om, pm = self.object_meta, self.proj_meta
+        nx, ny, nz = (int(s) for s in om.shape)
+        if nx != ny:
+            raise ValueError("rotate+sum needs Lx == Ly")
+        if tuple(pm.shape[1:]) != (ny, nz):
+            raise ValueError(f"projection shape {pm.shape[1:]} does not match object {om.shape}")
+        if not torch.cuda.is_available():
+            raise RuntimeError("SPECTSystemMatrix needs a CUDA device (no CPU path)")
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        n = pm.num_projections
+        Lp = om.padded_shape[0]
+        angles = pm.angles.to(torch.float32).cpu()
+        # forward rotation: RotationTransform.backward(obj, 270 - beta) -> rotate(beta - 270)
+        self._theta_fwd = geometry.rotation_theta(-(270 - angles), Lp)
+        # back-projection rotation: RotationTransform.forward(obj, 270 - beta)
+        self._theta_bwd = geometry.rotation_theta(270 - angles, Lp)
+        self._lin = geometry.base_grid(Lp)
+        order = ""
+        mu = None
+        psf_tables = None
+        self._transform_order = []
+        for t in self.obj2obj_transforms:
+            if isinstance(t, SPECTAttenuationTransform):
+                order += "a"
+                mu = t.attenuation_map.to(self.device, torch.float32).contiguous()
+            elif isinstance(t, SPECTPSFTransform):
+                order += "p"
+                psf_tables = t
+            else:
+                raise NotImplementedError(
+                    f"transform {type(t).__name__} has no fused GB300 implementation")
+        if order.count("a") > 1 or order.count("p") > 1:
+            raise NotImplementedError("at most one attenuation and one PSF transform")
+        self._order = order
+        self._mu = mu
+        desc = _lib.SpectDesc()
+        desc.nx, desc.ny, desc.nz = nx, ny, nz
+        desc.dx, desc.dy, desc.dz = (float(v) for v in om.dr)
+        desc.n_angles = n
+        keep = []
+
+        def host(t, dt=torch.float32):
+            a = t.to(dt).contiguous().cpu().numpy()
+            keep.append(a)
+            return a.ctypes.data_as(ctypes.c_void_p)
+
+        desc.theta_fwd = host(self._theta_fwd)
+        desc.theta_bwd = host(self._theta_bwd)
+        desc.lin = host(self._lin)
+        desc.mu = None if mu is None else ctypes.c_void_p(mu.data_ptr())
+        desc.order = order.encode()
+        if psf_tables is not None:
+            radii = psf_tables.radii_unique
+            group = np.array([radii.index(float(r)) for r in pm.radii], dtype=np.int32)
+            k = 1
+            two_d = True
+            for r in radii:
+                wr, wz = psf_tables.tables[r]
+                k = max(k, wr.shape[1], 0 if wz is None else wz.shape[1])
+                two_d = wz is not None
+            tr = np.zeros((len(radii), Lp, k), np.float32)
+            tz = np.zeros((len(radii), Lp, k), np.float32)
+            for gi, r in enumerate(radii):
+                wr, wz = psf_tables.tables[r]
+                o = (k - wr.shape[1]) // 2
+                tr[gi, :, o:o + wr.shape[1]] = wr.numpy()
+                if wz is not None:
+                    o = (k - wz.shape[1]) // 2
+                    tz[gi, :, o:o + wz.shape[1]] = wz.numpy()
+            keep.extend([tr, tz, group])
+            desc.psf_2d = 1 if two_d else 0
+            desc.psf_n_groups = len(radii)
+            desc.psf_group = group.ctypes.data_as(ctypes.c_void_p)
+            desc.psf_k = k
+            desc.psf_taps_r = tr.ctypes.data_as(ctypes.c_void_p)
+            desc.psf_taps_z = tz.ctypes.data_as(ctypes.c_void_p)
+            desc.psf_trunc_rel = self.psf_trunc_rel
+            self._psf_k = k
+        else:
+            self._psf_k = 1
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            torch.cuda.synchronize()
+            _lib.check(self._lib.gb_spect_plan_create(ctypes.byref(desc), ctypes.byref(handle)))
+        self._plan = handle
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None and self._lib is not None:
+            try:
+                self._lib.gb_spect_plan_destroy(plan)
+            except Exception:
+                pass
+            self._plan = None
+
+    # ------------------------------------------------------------ subsets
+    def set_n_subsets(self, n_subsets: int) -> None:
+        indices = torch.arange(self.proj_meta.shape[0]).to(torch.long).to(self.device)
+        self.subset_indices_array = [indices[i::n_subsets] for i in range(n_subsets)]
+        self.n_subsets = n_subsets
+        _lib.check(self._lib.gb_spect_set_subsets(self._plan, int(n_subsets)))
+
+    def get_projection_subset(self, projections: torch.Tensor, subset_idx: int) -> torch.Tensor:
+        return projections[..., self.subset_indices_array[subset_idx], :, :]
+
+    def get_weighting_subset(self, subset_idx: int | None) -> float:
+        if subset_idx is None:
+            return 1
+        return len(self.subset_indices_array[subset_idx]) / self.proj_meta.num_projections
+
+    def _subset_code(self, subset_idx) -> int:
+        if subset_idx is None:
+            return -1
+        if self.subset_indices_array is None:
+            raise RuntimeError("set_n_subsets must be called before using subset indices")
+        return int(subset_idx)
+
+    def _n_sel(self, subset_idx) -> int:
+        return self.proj_meta.num_projections if subset_idx is None else \
+            len(self.subset_indices_array[subset_idx])
+
+    # ------------------------------------------------------------ projectors
+    def _object_in(self, object: torch.Tensor) -> torch.Tensor:
+        obj = object.to(self.device, torch.float32)
+        if tuple(obj.shape) != tuple(self.object_meta.shape):
+            raise ValueError(f"object shape {tuple(obj.shape)} != {tuple(self.object_meta.shape)}")
+        return obj.contiguous()
+
+    def forward(self, object: torch.Tensor, subset_idx: int | None = None) -> torch.Tensor:
+        """H_m f -> [n_sel, Ly, Lz] (spect_system_matrix.py:120-157)."""
+        obj = self._object_in(object)
+        code = self._subset_code(subset_idx)
+        out = torch.empty((self._n_sel(subset_idx), *self.proj_meta.shape[1:]),
+                          device=self.device, dtype=torch.float32)
+        _lib.check(self._lib.gb_spect_forward(self._plan, _lib.ptr(obj), _lib.ptr(out), code,
+                                              _lib.stream_handle(self.device)))
+        return out
+
+    def _backward(self, proj: torch.Tensor, subset_idx, adjoint: int) -> torch.Tensor:
+        code = self._subset_code(subset_idx)
+        p = proj.to(self.device, torch.float32).contiguous()
+        exp = (self._n_sel(subset_idx), *self.proj_meta.shape[1:])
+        if tuple(p.shape) != exp:
+            raise ValueError(f"projection shape {tuple(p.shape)} != {exp}")
+        out = torch.empty(tuple(self.object_meta.shape), device=self.device, dtype=torch.float32)
+        _lib.check(self._lib.gb_spect_backward(self._plan, _lib.ptr(p), _lib.ptr(out), code,
+                                               adjoint, _lib.stream_handle(self.device)))
+        return out
+
+    def backward(self, proj: torch.Tensor, subset_idx: int | None = None) -> torch.Tensor:
+        """Reference back-projector (spect_system_matrix.py:159-201)."""
+        return self._backward(proj, subset_idx, 0)
+
+    def backward_adjoint(self, proj: torch.Tensor, subset_idx: int | None = None) -> torch.Tensor:
+        """Exact transpose of :meth:`forward` (same bilinear taps, scattered)."""
+        return self._backward(proj, subset_idx, 1)
+
+    def compute_normalization_factor(self, subset_idx: int | None = None) -> torch.Tensor:
+        n = self._n_sel(subset_idx)
+        ones = torch.ones((n, *self.proj_meta.shape[1:]), device=self.device)
+        return self.backward(ones, subset_idx)
+
+    # ------------------------------------------------------------ fused updates
+    def osem_step(self, object: torch.Tensor, projections: torch.Tensor,
+                  additive: torch.Tensor | None, norm_bp: torch.Tensor,
+                  subset_idx: int | None, predicted: torch.Tensor | None = None) -> None:
+        """In-place fused OSEM sub-iteration (see gb_spect_osem_step)."""
+        _lib.require_cuda(object, "object")
+        g = projections.to(self.device, torch.float32).contiguous()
+        s = None if additive is None else additive.to(self.device, torch.float32).contiguous()
+        nb = norm_bp.contiguous()
+        _lib.check(self._lib.gb_spect_osem_step(
+            self._plan, _lib.ptr(object), _lib.ptr(g), _lib.ptr(s), _lib.ptr(nb),
+            self._subset_code(subset_idx), _lib.ptr(predicted), _lib.stream_handle(self.device)))
+
+    def bsrem_step(self, object_in, object_out, projections, additive, norm_bp, norm_bp_sum,
+                   relax: float, subset_weight: float, prior=None, floor_value: float = 1e-4,
+                   subset_idx: int | None = None) -> None:
+        g = projections.contiguous()
+        s = None if additive is None else additive.contiguous()
+        rd = None
+        if prior is not None:
+            rd = _lib.RdpDesc(float(prior.beta), float(prior.gamma), float(prior.delta),
+                              None if prior.FOV_scale is None
+                              else ctypes.c_void_p(prior.FOV_scale.data_ptr()))
+        _lib.check(self._lib.gb_spect_bsrem_step(
+            self._plan, _lib.ptr(object_in), _lib.ptr(object_out), _lib.ptr(g), _lib.ptr(s),
+            _lib.ptr(norm_bp), _lib.ptr(norm_bp_sum), float(relax), float(subset_weight),
+            None if rd is None else ctypes.byref(rd), float(floor_value),
+            self._subset_code(subset_idx), _lib.stream_handle(self.device)))
+
+    # ------------------------------------------------------------ initial object
+    def _get_object_initial(self, device=None) -> torch.Tensor:
+        """Ones, optionally zeroed outside the camera path (spect_system_matrix.py:38-56)."""
+        dev = self.device if device is None else device
+        obj = torch.ones(tuple(self.object_meta.shape), device=dev)
+        if not self.object_initial_based_on_camera_path:
+            return obj
+        nx = self.object_meta.shape[0]
+        for i in range(len(self.proj_meta.angles)):
+            cutoff = int(np.ceil(nx / 2 - self.proj_meta.radii[i] / self.object_meta.dr[0]))
+            if cutoff < 0:
+                continue
+            cut = torch.ones(tuple(self.object_meta.shape), device=self.device)
+            cut[:cutoff] = 0
+            obj *= self._rotate_unpadded(cut, -(270 - float(self.proj_meta.angles[i]))).to(dev)
+        return obj
+
+    def _rotate_unpadded(self, x: torch.Tensor, angle: float) -> torch.Tensor:
+        """pad -> kornia-convention rotation -> unpad (setup-time helper, not the hot path)."""
+        pad = self.object_meta.pad_size
+        xp = torch.nn.functional.pad(x, [0, 0, pad, pad, pad, pad])
+        Lp = xp.shape[0]
+        theta = geometry.rotation_theta(torch.tensor([angle]), Lp).view(1, 2, 3).to(x.device)
+        img = xp.permute(2, 0, 1).unsqueeze(0)
+        grid = torch.nn.functional.affine_grid(theta, list(img.shape), align_corners=True)
+        r = torch.nn.functional.grid_sample(img, grid, mode="bilinear", padding_mode="zeros",
+                                            align_corners=True)
+        r = r.squeeze(0).permute(1, 2, 0)
+        return r[pad:-pad, pad:-pad, :]

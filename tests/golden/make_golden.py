@@ -188,8 +188,25 @@ def pet_meta_case(out):
     print("wrote pet_meta")
 
 
+def theta_case(out):
+    """Sampling matrices of the restated kornia rotation, for pinning the host tables."""
+    rec = {}
+    angles = torch.tensor([0.0, 3.7, 45.0, 90.0, 97.0, 180.0, 222.5, 270.0, 333.3, -270.0, -93.0],
+                          dtype=torch.float32)
+    for size in (23, 24, 92, 182):
+        th = refharness.kornia_sampling_matrix(
+            angles, torch.tensor([(size - 1) / 2.0, (size - 1) / 2.0]).expand(len(angles), 2),
+            size, size)
+        rec[f"theta_{size}"] = th.reshape(len(angles), 6).numpy()
+        rec[f"lin_{size}"] = torch.linspace(-1, 1, size).numpy()
+    rec["angles"] = angles.numpy()
+    np.savez_compressed(os.path.join(out, "theta.npz"), **rec)
+    print("wrote theta")
+
+
 def main():
     out = HERE
+    theta_case(out)
     torch.manual_seed(0)
     spect_case("spect_even", (16, 16, 12), (0.48, 0.48, 0.48),
                [float(a) for a in np.linspace(0, 360, 11)[:-1]],
