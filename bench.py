@@ -151,6 +151,8 @@ def main():
     ap.add_argument("--impl", default="gbtomo", choices=["gbtomo", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run 3 fused sub-iterations of the workload and exit (for ncu)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -184,6 +186,12 @@ def main():
     nbps = [nb.contiguous() for nb in lik.norm_BPs]
     f = torch.ones(w.shape, device=dev)
     n_sub = w.n_subsets
+    if args.profile_case:
+        for k in range(3):
+            H.osem_step(f, g, None, nbps[k], k)
+        torch.cuda.synchronize()
+        print("profile case done")
+        return
 
     # ---- plain per-call path (reference sequence through the drop-in projector)
     def plain_step(k):

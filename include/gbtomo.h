@@ -133,6 +133,63 @@ gb_status gb_rdp_gradient(const float *object, float *grad, int32_t nx, int32_t 
                           int32_t nz, float dx, float dy, float dz, const gb_rdp_desc *prior,
                           float beta_scale, gb_stream_t stream);
 
+/* -------------------------------------------------------------------- PET */
+
+typedef struct gb_pet_plan gb_pet_plan;
+
+/* Listmode geometry and events.  Mirrors PETLMProjMeta / PETTOFMeta
+ * (metadata/PET/petlm_metadata.py:6-39, metadata/PET/pet_tof_metadata.py:5-37) and the
+ * PETLMSystemMatrix constructor (projectors/PET/petlm_system_matrix.py:24-57). */
+typedef struct gb_pet_desc {
+    int32_t nx, ny, nz;        /* image shape [nx][ny][nz], z fastest */
+    float vx, vy, vz;          /* voxel size (mm) */
+    float ox, oy, oz;          /* centre of voxel (0,0,0) (mm): (-shape/2 + 0.5) * voxel */
+    int32_t n_det;             /* crystals in the scanner LUT */
+    const float *lut;          /* host [n_det][3] crystal centres (mm) */
+    int32_t tof;               /* 1: events carry a TOF bin in column 2 */
+    int32_t tof_num_bins;
+    float tof_bin_width;       /* mm */
+    float tof_sigma;           /* mm */
+    float tof_center_offset;   /* mm */
+    float tof_n_sigmas;
+    int64_t n_events;
+    const int32_t *events;     /* host or device [n_events][2 or 3]: id1, id2 (, tof bin) */
+} gb_pet_desc;
+
+/* Replaces PETLMSystemMatrix.__init__ (petlm_system_matrix.py:24-57) minus the
+ * sensitivity image (gb_pet_sensitivity).  Events are copied to the device once. */
+gb_status gb_pet_plan_create(const gb_pet_desc *desc, gb_pet_plan **plan);
+gb_status gb_pet_plan_destroy(gb_pet_plan *plan);
+/* Interleaved event subsets indices[i::n_subsets] (petlm_system_matrix.py:176-189). */
+gb_status gb_pet_set_subsets(gb_pet_plan *plan, int32_t n_subsets);
+
+/* TOF (or non-TOF) Joseph forward projection of the subset's events -> proj [n_sel].
+ * Replaces parallelproj.joseph3d_fwd_tof_lm / joseph3d_fwd as called by
+ * PETLMSystemMatrix.forward (petlm_system_matrix.py:243-297). */
+gb_status gb_pet_forward(gb_pet_plan *plan, const float *img, float *proj, int32_t subset,
+                         gb_stream_t stream);
+/* Adjoint: image (overwritten) = H_m^T proj.  Replaces joseph3d_back_tof_lm /
+ * joseph3d_back in PETLMSystemMatrix.backward (petlm_system_matrix.py:299-363). */
+gb_status gb_pet_backward(gb_pet_plan *plan, const float *proj, float *img, int32_t subset,
+                          gb_stream_t stream);
+/* Non-TOF line integrals of `img` along the subset's events (attenuation path,
+ * petlm_system_matrix.py:91-110); use_tof selects the TOF kernel instead. */
+gb_status gb_pet_lor_forward(gb_pet_plan *plan, const float *img, float *proj, int32_t subset,
+                             int32_t use_tof, gb_stream_t stream);
+/* Sensitivity image: non-TOF back projection of (weights * exp(-H mu) + add) over the
+ * LOR set `pairs` [n_pairs][2] (device), or over every crystal pair i < j when pairs is
+ * NULL (petlm_system_matrix.py:112-174).  weights / mu may be NULL. */
+gb_status gb_pet_sensitivity(gb_pet_plan *plan, const int32_t *pairs, int64_t n_pairs,
+                             const float *weights, const float *mu, float add, float *img,
+                             gb_stream_t stream);
+/* One fused listmode OSEM sub-iteration in place on img:
+ * f += f/(nbp+delta) * (H_m^T (numerator / (H_m f + s_m + delta)) - nbp), clamp at 0.
+ * numerator holds 1 value (listmode: projections = [1.]) or n_events values; additive
+ * (full [n_events], device) may be NULL; norm_bp is the subset's normalisation image. */
+gb_status gb_pet_osem_step(gb_pet_plan *plan, float *img, const float *numerator,
+                           int64_t numerator_len, const float *additive, const float *norm_bp,
+                           int32_t subset, gb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,6 +46,7 @@ class PetDesc(ctypes.Structure):
         ("n_det", c_int), ("lut", c_void_p),
         ("tof", c_int), ("tof_num_bins", c_int), ("tof_bin_width", c_float),
         ("tof_sigma", c_float), ("tof_center_offset", c_float), ("tof_n_sigmas", c_float),
+        ("n_events", ctypes.c_int64), ("events", c_void_p),
     ]
 
 
@@ -68,6 +69,16 @@ SIGNATURES = [
                                     c_float, c_int, c_void_p]),
     ("gb_rdp_gradient", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_float,
                                 c_float, ctypes.POINTER(RdpDesc), c_float, c_void_p]),
+    ("gb_pet_plan_create", c_int, [ctypes.POINTER(PetDesc), ctypes.POINTER(c_void_p)]),
+    ("gb_pet_plan_destroy", c_int, [c_void_p]),
+    ("gb_pet_set_subsets", c_int, [c_void_p, c_int]),
+    ("gb_pet_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("gb_pet_backward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("gb_pet_lor_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    ("gb_pet_sensitivity", c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
+                                   c_float, c_void_p, c_void_p]),
+    ("gb_pet_osem_step", c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_int64, c_void_p,
+                                 c_void_p, c_int, c_void_p]),
 ]
 
 

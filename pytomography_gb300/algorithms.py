@@ -52,9 +52,15 @@ class PreconditionedGradientAscentAlgorithm:
         self.object_prediction = self.callback.run(self.object_prediction, n_iter, n_subset)
 
     def _can_fuse(self) -> bool:
+        from .projectors.PET import PETLMSystemMatrix
         from .projectors.SPECT import SPECTSystemMatrix
-        ok = (isinstance(self.likelihood.system_matrix, SPECTSystemMatrix)
-              and type(self.likelihood) is PoissonLogLikelihood and self._fused_kind() is not None)
+        sm = self.likelihood.system_matrix
+        kind = self._fused_kind()
+        ok = (type(self.likelihood) is PoissonLogLikelihood and kind is not None
+              and (isinstance(sm, SPECTSystemMatrix)
+                   or (isinstance(sm, PETLMSystemMatrix) and kind == "osem"
+                       and not sm.scale_projection_by_sensitivity
+                       and sm.output_device == sm.device)))
         if self._fused_request is True and not ok:
             raise NotImplementedError("this likelihood / system matrix / prior has no fused step")
         return ok if self._fused_request is None else bool(self._fused_request)
@@ -128,6 +134,12 @@ class OSEM(LinearPreconditionedGradientAscentAlgorithm):
     def _fused_step(self, j, subset_idx):
         lik = self.likelihood
         sm = lik.system_matrix
+        from .projectors.PET import PETLMSystemMatrix
+        if isinstance(sm, PETLMSystemMatrix):
+            s = lik.additive_term if lik.exists_additive_term else None
+            sm.osem_step(self.object_prediction, lik.projections, s,
+                         lik._get_normBP(subset_idx), subset_idx)
+            return
         n_sel = sm._n_sel(subset_idx)
         pred = getattr(self, "_pred_buf", None)
         if pred is None or pred.shape[0] != n_sel:

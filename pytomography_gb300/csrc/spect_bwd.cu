@@ -56,7 +56,7 @@ cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_ang
 // Grid (chunk of planes, angle slot, z slab).  Output rows o <-> padded y = pad-H+o,
 // o in [0, N+2H); input S rows i <-> padded y = pad-2H+i (projection rows at i in
 // [2H, 2H+N), zero elsewhere).
-template <int K>
+template <int K, bool VEC>
 __global__ void __launch_bounds__(512, 1)
     k_b1_psf(SpectDev g, const float *__restrict__ proj, const int *__restrict__ alist,
              int n_chunks, int Zt, float *__restrict__ W) {
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(512, 1)
     const int Z8 = (Zc + OB - 1) / OB * OB;
     const int SC = Z8 + 2 * H, SR = O8 + 2 * H;     // S: [SR][SC]
     const int TS = O8 + 1, TR = Z8 + 2 * H;         // Tt: [TR][TS]
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     float *S = sm;
     float *Tt = S + SR * SC;
     float *tp = Tt + TR * TS;
@@ -134,9 +134,27 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
             for (int t = 0; t < K; t++) w[t] = tap[K + t];
             float *Wp = W + ((size_t)slot * g.Lp + xp) * g.nya * nz;
+            const bool amul = Ap && g.att_first;
             for (int task = threadIdx.x; task < n3; task += blockDim.x) {
-                int o_row = task % O8, zb = task / O8;
-                int y = g.pad - H + o_row;
+                const int o_row = task % O8, zb = task / O8;
+                const int y = g.pad - H + o_row;
+                const bool store = o_row < NO && y >= g.ya_lo && y < g.ya_hi;
+                const int zl0 = zb * OB;
+                const bool full = VEC && (zl0 + OB <= Zc);
+                const size_t rowoff = (size_t)(y - g.ya_lo) * nz + z0 + zl0;
+                float av[OB];
+                if (store && amul) {  // issue the A loads before the blur arithmetic
+                    if (full) {
+#pragma unroll
+                        for (int j = 0; j < OB; j += 4) {
+                            float4 a4 = __ldg(reinterpret_cast<const float4 *>(Ap + rowoff + j));
+                            av[j] = a4.x; av[j + 1] = a4.y; av[j + 2] = a4.z; av[j + 3] = a4.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < OB; j++) av[j] = zl0 + j < Zc ? Ap[rowoff + j] : 0.f;
+                    }
+                }
                 float o[OB];
                 if (g.psf2d) {
                     float win[OB + K - 1];
@@ -144,24 +162,29 @@ __global__ void __launch_bounds__(512, 1)
                     for (int i = 0; i < OB + K - 1; i++) win[i] = Tt[(zb * OB + i) * TS + o_row];
 #pragma unroll
                     for (int j = 0; j < OB; j++) {
-                        float s = 0.f;
+                        float s2 = 0.f;
 #pragma unroll
-                        for (int t = 0; t < K; t++) s = fmaf(w[t], win[j + t], s);
-                        o[j] = s;
+                        for (int t = 0; t < K; t++) s2 = fmaf(w[t], win[j + t], s2);
+                        o[j] = s2;
                     }
                 } else {
 #pragma unroll
                     for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + H) * TS + o_row];
                 }
-                if (o_row >= NO || y < g.ya_lo || y >= g.ya_hi) continue;
+                if (!store) continue;
+                if (amul) {
 #pragma unroll
-                for (int j = 0; j < OB; j++) {
-                    int zl = zb * OB + j;
-                    if (zl >= Zc) continue;
-                    int z = z0 + zl;
-                    float v = o[j];
-                    if (Ap && g.att_first) v = __fmul_rn(v, Ap[(size_t)(y - g.ya_lo) * nz + z]);
-                    Wp[(size_t)(y - g.ya_lo) * nz + z] = v;
+                    for (int j = 0; j < OB; j++) o[j] = __fmul_rn(o[j], av[j]);
+                }
+                if (full) {
+#pragma unroll
+                    for (int j = 0; j < OB; j += 4)
+                        *reinterpret_cast<float4 *>(Wp + rowoff + j) =
+                            make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < OB; j++)
+                        if (zl0 + j < Zc) Wp[rowoff + j] = o[j];
                 }
             }
         }
@@ -193,13 +216,19 @@ static cudaError_t launch_b1_psf_k(const SpectDev &g, const float *proj, const i
                                    int n_slots, int n_chunks, int Zt, float *W, cudaStream_t st) {
     size_t smem = b1_psf_smem_bytes(K, g.N, Zt);
     dim3 grid(n_chunks, n_slots, (g.nz + Zt - 1) / Zt);
-    k_b1_psf<K><<<grid, 512, smem, st>>>(g, proj, alist, n_chunks, Zt, W);
+    if (g.nz % 4 == 0)
+        k_b1_psf<K, true><<<grid, 512, smem, st>>>(g, proj, alist, n_chunks, Zt, W);
+    else
+        k_b1_psf<K, false><<<grid, 512, smem, st>>>(g, proj, alist, n_chunks, Zt, W);
     return cudaGetLastError();
 }
 
 template <int K>
 static cudaError_t setup_b1_k(size_t smem) {
-    return cudaFuncSetAttribute(k_b1_psf<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_b1_psf<K, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_b1_psf<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
 }
 
@@ -328,7 +357,52 @@ __device__ __forceinline__ void apply_update(int mode, const UpdateArgs &u, size
 
 // ------------------------------------------------------------- B2 gather
 // Reference back-projector: for every object voxel, bilinear sample of W at the
-// back-rotation (angle 270 - beta) of each angle of the group, summed.
+// back-rotation (angle 270 - beta) of each angle of the group, summed.  Threads own
+// (x, y, z quad); two angles are sampled before accumulating to keep loads in flight.
+__global__ void __launch_bounds__(256)
+    k_b2_gather4(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
+                 int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
+    const int q = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 8 + threadIdx.y;
+    const int x = blockIdx.z;
+    const int N = g.N, nz = g.nz;
+    if (4 * q >= nz || y >= N) return;
+    const int z = 4 * q;
+    const float lr = g.lin[x + g.pad], lc = g.lin[y + g.pad];
+    const size_t slab = (size_t)g.Lp * g.nya * nz;
+    float4 bp = make_float4(0.f, 0.f, 0.f, 0.f);
+    int s = 0;
+    for (; s + 1 < n_slots; s += 2) {
+        float ix, iy, ix2, iy2;
+        rot_coords(g.theta_bwd + 6 * alist[s], lr, lc, g.half, ix, iy);
+        rot_coords(g.theta_bwd + 6 * alist[s + 1], lr, lc, g.half, ix2, iy2);
+        Bilin b1 = bilin(ix, iy), b2 = bilin(ix2, iy2);
+        float4 v1, v2;
+        sample4(W + s * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b1, z, v1);
+        sample4(W + (s + 1) * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b2, z, v2);
+        bp.x = __fadd_rn(__fadd_rn(bp.x, v1.x), v2.x);
+        bp.y = __fadd_rn(__fadd_rn(bp.y, v1.y), v2.y);
+        bp.z = __fadd_rn(__fadd_rn(bp.z, v1.z), v2.z);
+        bp.w = __fadd_rn(__fadd_rn(bp.w, v1.w), v2.w);
+    }
+    if (s < n_slots) {
+        float ix, iy;
+        rot_coords(g.theta_bwd + 6 * alist[s], lr, lc, g.half, ix, iy);
+        Bilin b1 = bilin(ix, iy);
+        float4 v1;
+        sample4(W + s * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b1, z, v1);
+        bp.x = __fadd_rn(bp.x, v1.x);
+        bp.y = __fadd_rn(bp.y, v1.y);
+        bp.z = __fadd_rn(bp.z, v1.z);
+        bp.w = __fadd_rn(bp.w, v1.w);
+    }
+    const size_t i = ((size_t)x * N + y) * nz + z;
+    apply_update(mode, u, i, x, y, z, N, N, nz, bp.x, out);
+    apply_update(mode, u, i + 1, x, y, z + 1, N, N, nz, bp.y, out);
+    apply_update(mode, u, i + 2, x, y, z + 2, N, N, nz, bp.z, out);
+    apply_update(mode, u, i + 3, x, y, z + 3, N, N, nz, bp.w, out);
+}
+
 __global__ void __launch_bounds__(256)
     k_b2_gather(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
                 int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
@@ -355,8 +429,13 @@ __global__ void __launch_bounds__(256)
 cudaError_t launch_b2_gather(const SpectDev &g, const float *W, const int *alist, int n_slots,
                              float *out, int mode, const UpdateArgs &u, cudaStream_t st) {
     dim3 block(32, 8);
-    dim3 grid((g.nz + 31) / 32, (g.N + 7) / 8, g.N);
-    k_b2_gather<<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
+    if (g.nz % 4 == 0) {
+        dim3 grid((g.nz / 4 + 31) / 32, (g.N + 7) / 8, g.N);
+        k_b2_gather4<<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
+    } else {
+        dim3 grid((g.nz + 31) / 32, (g.N + 7) / 8, g.N);
+        k_b2_gather<<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
+    }
     return cudaGetLastError();
 }
 

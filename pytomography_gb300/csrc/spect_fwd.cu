@@ -42,11 +42,18 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 }
 
 // ---------------------------------------------------------------- with PSF
-template <int K>
+// Shared-memory layout (per CTA):
+//   S  [SR][SC]: rotated, attenuated samples; row r <-> padded y = pad - H + r,
+//                column c <-> z = z0 - HP + c  (HP = H rounded up to 4: 16-byte aligned
+//                z quads)
+//   Tt [TR][TS]: y-blurred plane, transposed; row c <-> z = z0 - HP + c, column = output y
+//   taps [2][2][K]: double-buffered y / z taps of the current plane
+template <int K, bool VEC>
 __global__ void __launch_bounds__(512, 1)
     k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
               int n_chunks, int Zt, float *__restrict__ partials) {
     constexpr int H = K / 2;
+    constexpr int HP = (H + 3) / 4 * 4;
     constexpr int OB = (K <= 31) ? 8 : 4;  // outputs per task
     constexpr int NACC = 32 / OB;          // phase-3 tasks per thread
     const int slot = blockIdx.y, chunk = blockIdx.x;
@@ -56,12 +63,12 @@ __global__ void __launch_bounds__(512, 1)
     const int Zc = min(Zt, nz - z0);
     const int N8 = (N + OB - 1) / OB * OB;
     const int Z8 = (Zc + OB - 1) / OB * OB;
-    const int SC = Z8 + 2 * H, SR = N8 + 2 * H;  // S: [SR][SC], col c <-> z = z0-H+c
-    const int TS = N8 + 1, TR = Z8 + 2 * H;      // Tt: [TR][TS], row c <-> z = z0-H+c
-    extern __shared__ float sm[];
+    const int SC = Z8 + 2 * HP, SR = N8 + 2 * H;
+    const int TS = N8 + 1, TR = Z8 + 2 * HP;
+    extern __shared__ __align__(16) float sm[];
     float *S = sm;
     float *Tt = S + SR * SC;
-    float *tp = Tt + TR * TS;  // [2 buffers][2 (r,z)][K]
+    float *tp = Tt + TR * TS;
     for (int i = threadIdx.x; i < SR * SC + TR * TS; i += blockDim.x) sm[i] = 0.f;
 
     float th[6];
@@ -70,10 +77,15 @@ __global__ void __launch_bounds__(512, 1)
     const int grp = g.group[ga];
     const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
     const int x0 = chunk * g.Lp / n_chunks, x1 = (chunk + 1) * g.Lp / n_chunks;
-    const int cz_lo = max(0, H - z0), cz_hi = min(SC, nz - z0 + H);
+    const int zv_lo = max(0, z0 - H), zv_hi = min(nz, z0 + Zc + H);  // z needed by the blur
+    const int cz_lo = zv_lo - z0 + HP, cz_hi = zv_hi - z0 + HP;
     const int ncol = cz_hi - cz_lo;
     const int ylo = max(0, g.pad - H), yhi = min(g.Lp, g.pad + N + H);  // sampled rows
     const int n3 = N8 * (Z8 / OB);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    // z quads covering [zv_lo, zv_hi) (vector path)
+    const int zq_lo = zv_lo & ~3, zq_hi = (zv_hi + 3) & ~3;
+    const int nq = (zq_hi - zq_lo) >> 2;
     float acc[NACC][OB];
 #pragma unroll
     for (int k = 0; k < NACC; k++)
@@ -93,15 +105,44 @@ __global__ void __launch_bounds__(512, 1)
         }
         // phase 1: rotated samples (times A when attenuation precedes the PSF)
         const float *Ap = A ? A + (size_t)xp * g.nya * nz : nullptr;
-        for (int i = threadIdx.x; i < (yhi - ylo) * ncol; i += blockDim.x) {
-            int y = ylo + i / ncol, c = cz_lo + i % ncol;
-            int z = z0 - H + c;
-            float ix, iy;
-            rot_coords(th, lr, g.lin[y], g.half, ix, iy);
-            Bilin b = bilin(ix, iy);
-            float v = sample(f, N, N, nz, g.pad, g.pad, b, z);
-            if (Ap && g.att_first) v = __fmul_rn(v, Ap[(size_t)(y - g.ya_lo) * nz + z]);
-            S[(y - (g.pad - H)) * SC + c] = v;
+        const bool amul = Ap && g.att_first;
+        if (VEC) {
+            // one row per warp, two rows in flight, z quads across lanes
+            for (int y = ylo + warp; y < yhi; y += 2 * nwarp) {
+                const int y2 = y + nwarp;
+                const bool two = y2 < yhi;
+                float ix, iy, ix2, iy2;
+                rot_coords(th, lr, g.lin[y], g.half, ix, iy);
+                rot_coords(th, lr, g.lin[two ? y2 : y], g.half, ix2, iy2);
+                const Bilin b1 = bilin(ix, iy), b2 = bilin(ix2, iy2);
+                float *S1 = S + (y - (g.pad - H)) * SC;
+                float *S2 = S + (y2 - (g.pad - H)) * SC;
+                for (int q = lane; q < nq; q += 32) {
+                    const int z = zq_lo + 4 * q;
+                    float4 v1, v2;
+                    bool h1 = sample4(f, N, N, nz, g.pad, g.pad, b1, z, v1);
+                    bool h2 = two && sample4(f, N, N, nz, g.pad, g.pad, b2, z, v2);
+                    if (amul && h1)
+                        v1 = mul4(v1, __ldg(reinterpret_cast<const float4 *>(
+                                          Ap + (size_t)(y - g.ya_lo) * nz + z)));
+                    if (amul && h2)
+                        v2 = mul4(v2, __ldg(reinterpret_cast<const float4 *>(
+                                          Ap + (size_t)(y2 - g.ya_lo) * nz + z)));
+                    *reinterpret_cast<float4 *>(S1 + (z - z0 + HP)) = v1;
+                    if (two) *reinterpret_cast<float4 *>(S2 + (z - z0 + HP)) = h2 ? v2 : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+        } else {
+            for (int i = threadIdx.x; i < (yhi - ylo) * ncol; i += blockDim.x) {
+                int y = ylo + i / ncol, c = cz_lo + i % ncol;
+                int z = z0 - HP + c;
+                float ix, iy;
+                rot_coords(th, lr, g.lin[y], g.half, ix, iy);
+                Bilin b = bilin(ix, iy);
+                float v = sample(f, N, N, nz, g.pad, g.pad, b, z);
+                if (amul && v != 0.f) v = __fmul_rn(v, Ap[(size_t)(y - g.ya_lo) * nz + z]);
+                S[(y - (g.pad - H)) * SC + c] = v;
+            }
         }
         __syncthreads();
         // phase 2: blur along y, write transposed
@@ -138,7 +179,8 @@ __global__ void __launch_bounds__(512, 1)
                     if (g.psf2d) {
                         float win[OB + K - 1];
 #pragma unroll
-                        for (int i = 0; i < OB + K - 1; i++) win[i] = Tt[(zb * OB + i) * TS + y];
+                        for (int i = 0; i < OB + K - 1; i++)
+                            win[i] = Tt[(zb * OB + i + HP - H) * TS + y];
 #pragma unroll
                         for (int j = 0; j < OB; j++) {
                             float s = 0.f;
@@ -148,7 +190,7 @@ __global__ void __launch_bounds__(512, 1)
                         }
                     } else {
 #pragma unroll
-                        for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + H) * TS + y];
+                        for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + HP) * TS + y];
                     }
                     if (Ap && !g.att_first && y < N) {
 #pragma unroll
@@ -240,32 +282,33 @@ __global__ void k_reduce(int n_chunks, int NZ, const float *__restrict__ partial
 }
 
 // ------------------------------------------------------------- launchers
+size_t fwd_psf_smem_bytes(int K, int N, int Zt) {
+    int H = K / 2, HP = (H + 3) / 4 * 4, OB = (K <= 31) ? 8 : 4;
+    int N8 = (N + OB - 1) / OB * OB;
+    int Z8 = (Zt + OB - 1) / OB * OB;
+    return sizeof(float) *
+           ((size_t)(N8 + 2 * H) * (Z8 + 2 * HP) + (size_t)(Z8 + 2 * HP) * (N8 + 1) + 4 * K);
+}
+
 template <int K>
 static cudaError_t launch_fwd_psf_k(const SpectDev &g, const float *f, const int *alist,
                                     int n_slots, int n_chunks, int Zt, float *partials,
                                     cudaStream_t st) {
-    constexpr int H = K / 2;
-    constexpr int OB = (K <= 31) ? 8 : 4;
-    int N8 = (g.N + OB - 1) / OB * OB;
-    int Z8 = (Zt + OB - 1) / OB * OB;
-    size_t smem = sizeof(float) *
-                  ((size_t)(N8 + 2 * H) * (Z8 + 2 * H) + (size_t)(Z8 + 2 * H) * (N8 + 1) + 4 * K);
+    size_t smem = fwd_psf_smem_bytes(K, g.N, Zt);
     dim3 grid(n_chunks, n_slots, (g.nz + Zt - 1) / Zt);
-    k_fwd_psf<K><<<grid, 512, smem, st>>>(g, f, alist, n_chunks, Zt, partials);
+    if (g.nz % 4 == 0)
+        k_fwd_psf<K, true><<<grid, 512, smem, st>>>(g, f, alist, n_chunks, Zt, partials);
+    else
+        k_fwd_psf<K, false><<<grid, 512, smem, st>>>(g, f, alist, n_chunks, Zt, partials);
     return cudaGetLastError();
-}
-
-size_t fwd_psf_smem_bytes(int K, int N, int Zt) {
-    int H = K / 2, OB = (K <= 31) ? 8 : 4;
-    int N8 = (N + OB - 1) / OB * OB;
-    int Z8 = (Zt + OB - 1) / OB * OB;
-    return sizeof(float) *
-           ((size_t)(N8 + 2 * H) * (Z8 + 2 * H) + (size_t)(Z8 + 2 * H) * (N8 + 1) + 4 * K);
 }
 
 template <int K>
 static cudaError_t setup_fwd_k(size_t smem) {
-    return cudaFuncSetAttribute(k_fwd_psf<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_fwd_psf<K, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_fwd_psf<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
 }
 

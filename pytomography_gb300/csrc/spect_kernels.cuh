@@ -114,4 +114,33 @@ __device__ __forceinline__ float sample(const float *__restrict__ src, int rows,
     return bilin_combine(b, vnw, vne, vsw, vse);
 }
 
+// Four consecutive z values (z % 4 == 0, nz % 4 == 0) of the bilinear sample; returns
+// false (and zeros) when no tap is inside the array.
+__device__ __forceinline__ bool sample4(const float *__restrict__ src, int rows, int cols, int nz,
+                                        int row_off, int col_off, const Bilin &b, int z,
+                                        float4 &out) {
+    int r = b.r0 - row_off, c = b.c0 - col_off;
+    bool r0 = (unsigned)r < (unsigned)rows, r1 = (unsigned)(r + 1) < (unsigned)rows;
+    bool c0 = (unsigned)c < (unsigned)cols, c1 = (unsigned)(c + 1) < (unsigned)cols;
+    out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!((r0 || r1) && (c0 || c1))) return false;
+    const float *p = src + ((long long)r * cols + c) * nz + z;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 vnw = (r0 && c0) ? __ldg(reinterpret_cast<const float4 *>(p)) : zero;
+    float4 vne = (r0 && c1) ? __ldg(reinterpret_cast<const float4 *>(p + nz)) : zero;
+    float4 vsw = (r1 && c0) ? __ldg(reinterpret_cast<const float4 *>(p + (long long)cols * nz)) : zero;
+    float4 vse = (r1 && c1) ? __ldg(reinterpret_cast<const float4 *>(p + (long long)cols * nz + nz))
+                            : zero;
+    out.x = bilin_combine(b, vnw.x, vne.x, vsw.x, vse.x);
+    out.y = bilin_combine(b, vnw.y, vne.y, vsw.y, vse.y);
+    out.z = bilin_combine(b, vnw.z, vne.z, vsw.z, vse.z);
+    out.w = bilin_combine(b, vnw.w, vne.w, vsw.w, vse.w);
+    return true;
+}
+
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) {
+    return make_float4(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z),
+                       __fmul_rn(a.w, b.w));
+}
+
 }  // namespace gb

@@ -1,0 +1,204 @@
+"""Drop-in ``PETLMSystemMatrix`` on the sm_103a TOF Joseph listmode kernels.
+
+Mirror of src/pytomography/projectors/PET/petlm_system_matrix.py:11-363.  Events and the
+scanner LUT are uploaded once and stay resident on the GPU (the reference gathers LUT rows
+on the CPU and copies them to the device on every call); subsets ``i::n`` are addressed
+by stride inside the kernels, so no gather copies are made.  The sensitivity image
+generates every crystal pair on the device instead of materialising torch.combinations.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .system_matrix import SystemMatrix
+
+
+class PETLMSystemMatrix(SystemMatrix):
+    def __init__(self, object_meta, proj_meta, obj2obj_transforms=None,
+                 attenuation_map: torch.Tensor | None = None,
+                 scale_projection_by_sensitivity: bool = False, N_splits: int = 1,
+                 FOV_scale_enabled: bool = True, device=None,
+                 compute_sensitivity: bool = True) -> None:
+        if obj2obj_transforms:
+            raise NotImplementedError("PET obj2obj transforms are not part of the fused path")
+        super().__init__(object_meta, proj_meta, [], [])
+        if not torch.cuda.is_available():
+            raise RuntimeError("PETLMSystemMatrix needs a CUDA device (no CPU path)")
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        self.output_device = self.device if device is None else torch.device(device)
+        self.TOF = proj_meta.tof_meta is not None
+        self.object_origin = (-np.array(object_meta.shape) / 2 + 0.5) * np.array(object_meta.dr)
+        self.proj_meta.detector_ids = self.proj_meta.detector_ids.cpu()
+        self.proj_meta.scanner_lut = self.proj_meta.scanner_lut.cpu()
+        self.attenuation_map = attenuation_map
+        self.N_splits = N_splits
+        self.scale_projection_by_sensitivity = scale_projection_by_sensitivity
+        self.FOV_scale_enabled = FOV_scale_enabled
+        self._lib = _lib.load()
+        self._build_plan()
+        self.subset_indices_array = None
+        self.n_subsets = 1
+        if compute_sensitivity:
+            self.norm_BP = self._backward_full()
+            self.norm_BP[self.norm_BP < 1e-7] = 1e7
+        else:
+            self.norm_BP = None
+
+    def _build_plan(self):
+        om, pm = self.object_meta, self.proj_meta
+        d = _lib.PetDesc()
+        d.nx, d.ny, d.nz = (int(s) for s in om.shape)
+        d.vx, d.vy, d.vz = (float(v) for v in om.dr)
+        d.ox, d.oy, d.oz = (float(v) for v in self.object_origin)
+        lut = pm.scanner_lut.to(torch.float32).contiguous().numpy()
+        d.n_det = lut.shape[0]
+        d.lut = lut.ctypes.data_as(ctypes.c_void_p)
+        ncol = 3 if self.TOF else 2
+        ids = pm.detector_ids[:, :ncol].to(torch.int32).contiguous()
+        self._ids_dev = ids.to(self.device)
+        d.n_events = ids.shape[0]
+        d.events = ctypes.c_void_p(self._ids_dev.data_ptr())
+        if self.TOF:
+            t = pm.tof_meta
+            d.tof = 1
+            d.tof_num_bins = int(t.num_bins)
+            d.tof_bin_width = float(t.bin_width)
+            d.tof_sigma = float(t.sigma)
+            d.tof_center_offset = float(t.center_offset)
+            d.tof_n_sigmas = float(t.n_sigmas)
+        h = ctypes.c_void_p()
+        torch.cuda.synchronize()
+        _lib.check(self._lib.gb_pet_plan_create(ctypes.byref(d), ctypes.byref(h)))
+        self._plan = h
+        self._keep = (lut, ids)
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None and getattr(self, "_lib", None) is not None:
+            try:
+                self._lib.gb_pet_plan_destroy(plan)
+            except Exception:
+                pass
+            self._plan = None
+
+    # ------------------------------------------------------------ FOV helpers
+    def _z_fov(self):
+        lut_z = self.proj_meta.scanner_lut[:, 2]
+        nzv = self.object_meta.shape[-1]
+        zmin = (nzv - 1) / 2 + float(lut_z.min()) / self.object_meta.dr[-1]
+        zmax = (nzv - 1) / 2 + float(lut_z.max()) / self.object_meta.dr[-1]
+        return zmin, zmax
+
+    def _get_object_initial(self, device=None):
+        zmin, zmax = self._z_fov()
+        zmin, zmax = max(0, zmin), max(0, zmax)
+        obj = torch.ones(tuple(self.object_meta.shape)).to(self.device if device is None else device)
+        obj[:, :, :int(np.ceil(zmin))] = 0
+        obj[:, :, int(np.floor(zmax)):] = 0
+        return obj
+
+    def _get_prior_FOV_scale(self):
+        if not self.FOV_scale_enabled:
+            return torch.ones(tuple(self.object_meta.shape)).to(self.device)
+        zmin, zmax = self._z_fov()
+        zmid = (zmin + zmax) / 2
+        z = torch.arange(self.object_meta.shape[-1]).to(self.device)
+        fov = (zmid - torch.abs(z - zmid)) / zmid
+        fov[fov < 0] = 0
+        return torch.ones(tuple(self.object_meta.shape)).to(self.device) * fov
+
+    # ------------------------------------------------------------ subsets
+    def set_n_subsets(self, n_subsets: int) -> None:
+        idx = torch.arange(self.proj_meta.detector_ids.shape[0]).to(torch.long).cpu()
+        self.subset_indices_array = [idx[i::n_subsets] for i in range(n_subsets)]
+        self.n_subsets = n_subsets
+        _lib.check(self._lib.gb_pet_set_subsets(self._plan, int(n_subsets)))
+
+    def get_projection_subset(self, projections, subset_idx):
+        if projections.shape[0] > 1 and subset_idx is not None:
+            return projections[self.subset_indices_array[subset_idx]]
+        return projections
+
+    def get_weighting_subset(self, subset_idx):
+        if subset_idx is None:
+            return 1
+        return len(self.subset_indices_array[subset_idx]) / self.proj_meta.detector_ids.shape[0]
+
+    def compute_normalization_factor(self, subset_idx=None):
+        frac = 1 if subset_idx is None else \
+            self.subset_indices_array[subset_idx].shape[0] / self.proj_meta.detector_ids.shape[0]
+        return frac * self.norm_BP.to(self.output_device)
+
+    def _code(self, subset_idx):
+        if subset_idx is None:
+            return -1
+        if self.subset_indices_array is None:
+            raise RuntimeError("set_n_subsets must be called before using subset indices")
+        return int(subset_idx)
+
+    def _n_sel(self, subset_idx):
+        return self.proj_meta.detector_ids.shape[0] if subset_idx is None else \
+            len(self.subset_indices_array[subset_idx])
+
+    # ------------------------------------------------------------ projectors
+    def _weights(self, subset_idx):
+        if self.proj_meta.weights is None:
+            raise Exception("If scaling by sensitivity, then `weights` must be provided in the "
+                            "projection metadata")
+        return self.get_projection_subset(self.proj_meta.weights, subset_idx).to(self.device)
+
+    def forward(self, object, subset_idx=None):
+        img = object.to(self.device, torch.float32).contiguous()
+        out = torch.empty(self._n_sel(subset_idx), device=self.device)
+        _lib.check(self._lib.gb_pet_forward(self._plan, _lib.ptr(img), _lib.ptr(out),
+                                            self._code(subset_idx), _lib.stream_handle(self.device)))
+        if self.scale_projection_by_sensitivity:
+            out = out * self._weights(subset_idx)
+        return out.to(self.output_device)
+
+    def backward(self, proj, subset_idx=None, return_norm_constant: bool = False):
+        p = proj.to(self.device, torch.float32)
+        if self.scale_projection_by_sensitivity:
+            p = p * self._weights(subset_idx)
+        p = p.contiguous()
+        out = torch.empty(tuple(self.object_meta.shape), device=self.device)
+        _lib.check(self._lib.gb_pet_backward(self._plan, _lib.ptr(p), _lib.ptr(out),
+                                             self._code(subset_idx), _lib.stream_handle(self.device)))
+        if return_norm_constant:
+            return out.to(self.output_device), self.compute_normalization_factor(subset_idx)
+        return out.to(self.output_device)
+
+    def osem_step(self, object, numerator, additive, norm_bp, subset_idx):
+        """Fused listmode OSEM sub-iteration in place on ``object``."""
+        num = numerator.to(self.device, torch.float32).contiguous()
+        s = None if additive is None else additive.to(self.device, torch.float32).contiguous()
+        _lib.check(self._lib.gb_pet_osem_step(self._plan, _lib.ptr(object), _lib.ptr(num),
+                                              int(num.numel()), _lib.ptr(s),
+                                              _lib.ptr(norm_bp.contiguous()),
+                                              self._code(subset_idx),
+                                              _lib.stream_handle(self.device)))
+
+    # ------------------------------------------------------------ sensitivity
+    def _backward_full(self) -> torch.Tensor:
+        """H~^T (w a + delta) over the sensitivity LOR set (petlm_system_matrix.py:112-174)."""
+        pm = self.proj_meta
+        pairs = None
+        n_pairs = 0
+        if pm.detector_ids_sensitivity is not None:
+            pairs = pm.detector_ids_sensitivity[:, :2].to(torch.int32).contiguous().to(self.device)
+            n_pairs = pairs.shape[0]
+        w = None
+        if pm.weights_sensitivity is not None:
+            w = pm.weights_sensitivity.to(self.device, torch.float32).contiguous()
+        mu = None
+        if self.attenuation_map is not None:
+            mu = self.attenuation_map.to(self.device, torch.float32).contiguous()
+        out = torch.empty(tuple(self.object_meta.shape), device=self.device)
+        _lib.check(self._lib.gb_pet_sensitivity(self._plan, _lib.ptr(pairs), int(n_pairs),
+                                                _lib.ptr(w), _lib.ptr(mu), float(1e-11),
+                                                _lib.ptr(out), _lib.stream_handle(self.device)))
+        return out
