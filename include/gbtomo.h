@@ -76,6 +76,11 @@ typedef struct gb_spect_desc {
 gb_status gb_spect_plan_create(const gb_spect_desc *desc, gb_spect_plan **plan);
 gb_status gb_spect_plan_destroy(gb_spect_plan *plan);
 
+/* Device-side error word of the plan (synchronous read): 0, or 1 when a kernel's
+ * bounded wait on its TMA copies gave up (the kernel then returned without output).
+ * No counterpart in the reference (which has no device code). */
+gb_status gb_spect_device_status(gb_spect_plan *plan, int32_t *code);
+
 /* Interleaved angle subsets indices[i::n_subsets]
  * (spect_system_matrix.py:58-71).  n_subsets >= 1. */
 gb_status gb_spect_set_subsets(gb_spect_plan *plan, int32_t n_subsets);
@@ -87,6 +92,7 @@ int32_t gb_spect_subset_size(const gb_spect_plan *plan, int32_t subset);
  * subset = -1 projects every angle. */
 gb_status gb_spect_forward(gb_spect_plan *plan, const float *object, float *proj,
                            int32_t subset, gb_stream_t stream);
+
 
 /* Back projection proj [n_sel][ny][nz] -> object [nx][ny][nz] (device, overwritten).
  * adjoint = 0: the reference back-projector, which rotates back with bilinear

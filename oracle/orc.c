@@ -266,9 +266,15 @@ static REAL joseph(int back, const REAL *p0, const REAL *p1, REAL *img, const in
     REAL d[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
     REAL len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     if (len == 0) return 0;
+    /* principal axis from exact differences of the end points (ties such as
+     * |dx| == |dy| resolve as in exact arithmetic, whatever REAL is) */
     int k = 0;
-    if (fabs(d[1]) > fabs(d[k])) k = 1;
-    if (fabs(d[2]) > fabs(d[k])) k = 2;
+    {
+        double e[3] = {fabs((double)p1[0] - (double)p0[0]), fabs((double)p1[1] - (double)p0[1]),
+                       fabs((double)p1[2] - (double)p0[2])};
+        if (e[1] > e[0]) k = 1;
+        if (e[2] > e[k]) k = 2;
+    }
     int a = (k + 1) % 3, b = (k + 2) % 3;
     REAL cf = vox[k] * len / fabs(d[k]);
     REAL u[3] = {d[0] / len, d[1] / len, d[2] / len};

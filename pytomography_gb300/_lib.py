@@ -59,6 +59,7 @@ SIGNATURES = [
     ("gb_spect_plan_create", c_int, [ctypes.POINTER(SpectDesc), ctypes.POINTER(c_void_p)]),
     ("gb_spect_plan_destroy", c_int, [c_void_p]),
     ("gb_spect_set_subsets", c_int, [c_void_p, c_int]),
+    ("gb_spect_device_status", c_int, [c_void_p, ctypes.POINTER(c_int)]),
     ("gb_spect_subset_size", c_int, [c_void_p, c_int]),
     ("gb_spect_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("gb_spect_backward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),

@@ -54,9 +54,15 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
     const float dx = p1[0] - ax, dy = p1[1] - ay, dz = p1[2] - az;
     const float len = sqrtf(dx * dx + dy * dy + dz * dz);
     if (len == 0.f) return 0.f;
+    // principal axis from exact (double) differences of the float end points, so that
+    // ties such as |dx| == |dy| resolve the same way as in exact arithmetic
     int k = 0;
-    if (fabsf(dy) > fabsf(dx)) k = 1;
-    if (fabsf(dz) > fabsf(pick(dx, dy, dz, k))) k = 2;
+    {
+        const double ex = fabs((double)p1[0] - (double)ax), ey = fabs((double)p1[1] - (double)ay),
+                     ez = fabs((double)p1[2] - (double)az);
+        if (ey > ex) k = 1;
+        if (ez > (k == 0 ? ex : ey)) k = 2;
+    }
     const int a = (k + 1) % 3, b = (k + 2) % 3;
     const int strides[3] = {g.n[1] * g.n[2], g.n[2], 1};
     const float dk = pick(dx, dy, dz, k), da = pick(dx, dy, dz, a), db = pick(dx, dy, dz, b);
@@ -102,7 +108,10 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
         if (TOF) {
             const float s = (t - 0.5f) * len - tc;
             if (fabsf(s) > lim) continue;
-            w *= 0.5f * (erff((s + hb) * isq) - erff((s - hb) * isq));
+            // (erf((s+h)q) - erf((s-h)q))/2 written with erfc of |s| (same value by
+            // symmetry) so the Gaussian tails do not cancel in float32
+            const float as = fabsf(s);
+            w *= 0.5f * (erfcf((as - hb) * isq) - erfcf((as + hb) * isq));
         }
         const float pa = pa0 + t * da, pb = pb0 + t * db;
         const float fa = (pa - oa) / va, fb = (pb - ob) / vb;

@@ -18,6 +18,8 @@
 
 namespace gb {
 
+static bool b1_fixed(int K, int N, int Zt);
+
 // ------------------------------------------------------------- attenuation
 // A[a][xp][y][z] = exp(-(sum_{k>=xp} mu_rot[k]*dx - mu_rot[xp]*dx/2)) for the stored
 // rows y in [ya_lo, ya_hi); mu_rot uses the forward rotation of angle a.
@@ -56,22 +58,25 @@ cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_ang
 // Grid (chunk of planes, angle slot, z slab).  Output rows o <-> padded y = pad-H+o,
 // o in [0, N+2H); input S rows i <-> padded y = pad-2H+i (projection rows at i in
 // [2H, 2H+N), zero elsewhere).
-template <int K, bool VEC>
+// FIXED: N <= 128 and a z slab <= 128 wide: compile-time shared-memory strides.
+template <int K, bool VEC, bool FIXED>
 __global__ void __launch_bounds__(512, 1)
     k_b1_psf(SpectDev g, const float *__restrict__ proj, const int *__restrict__ alist,
-             int n_chunks, int Zt, float *__restrict__ W) {
+             const int4 *__restrict__ items, int Zt, float *__restrict__ W) {
     constexpr int H = K / 2;
     constexpr int OB = (K <= 31) ? 8 : 4;
-    const int slot = blockIdx.y, chunk = blockIdx.x;
+    const int4 item = items[blockIdx.x];  // (slot in group, first plane, end plane)
+    const int slot = item.x;
     const int ga = alist[slot];
     const int N = g.N, nz = g.nz;
-    const int z0 = blockIdx.z * Zt;
+    const int z0 = blockIdx.y * Zt;
     const int Zc = min(Zt, nz - z0);
     const int NO = N + 2 * H;                       // output rows
     const int O8 = (NO + OB - 1) / OB * OB;
     const int Z8 = (Zc + OB - 1) / OB * OB;
-    const int SC = Z8 + 2 * H, SR = O8 + 2 * H;     // S: [SR][SC]
-    const int TS = O8 + 1, TR = Z8 + 2 * H;         // Tt: [TR][TS]
+    constexpr int O8_FIX = (128 + 2 * H + OB - 1) / OB * OB;
+    const int SC = FIXED ? 128 + 2 * H : Z8 + 2 * H, SR = O8 + 2 * H;  // S: [SR][SC]
+    const int TS = FIXED ? O8_FIX + 1 : O8 + 1, TR = Z8 + 2 * H;        // Tt: [TR][TS]
     extern __shared__ __align__(16) float sm[];
     float *S = sm;
     float *Tt = S + SR * SC;
@@ -79,8 +84,9 @@ __global__ void __launch_bounds__(512, 1)
     for (int i = threadIdx.x; i < SR * SC + TR * TS; i += blockDim.x) sm[i] = 0.f;
     const int grp = g.group[ga];
     const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
-    const int x0 = chunk * g.Lp / n_chunks, x1 = (chunk + 1) * g.Lp / n_chunks;
-    const int cz_lo = max(0, H - z0), cz_hi = min(SC, nz - z0 + H);
+    const int x0 = item.y, x1 = item.z;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    const int cz_lo = max(0, H - z0), cz_hi = min(Z8 + 2 * H, nz - z0 + H);
     const int ncol = cz_hi - cz_lo;
     const float *P = proj + (size_t)slot * N * nz;
     const bool att_inside = A && !g.att_first;  // "pa": A multiplies before the blur
@@ -91,9 +97,21 @@ __global__ void __launch_bounds__(512, 1)
             S[(2 * H + y) * SC + c] = P[(size_t)y * nz + (z0 - H + c)];
         }
     }
-    const int n3 = O8 * (Z8 / OB);
+    float th[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * ga + k];
+    int2 *wr = g.wrange + (size_t)slot * g.Lp;
     int parity = 0;
     for (int xp = x0; xp < x1; ++xp) {
+        // rows of this plane the gather can sample (object square + 1.5 px margin)
+        int ra, rb;
+        if (!plane_rows(g, th, xp, g.ya_lo, g.ya_hi, 1.5f, ra, rb)) {
+            if (threadIdx.x == 0) wr[xp] = make_int2(0, 0);
+            continue;
+        }
+        if (threadIdx.x == 0) wr[xp] = make_int2(ra - g.ya_lo, rb + 1 - g.ya_lo);
+        const int o_lo = ra - (g.pad - H), o_hi = rb - (g.pad - H) + 1;  // output rows
+        const int b_lo = o_lo / OB, b_hi = (o_hi + OB - 1) / OB;
         float *tap = tp + parity * 2 * K;
         if (threadIdx.x < K) {
             tap[threadIdx.x] = g.taps_r[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x];
@@ -114,17 +132,23 @@ __global__ void __launch_bounds__(512, 1)
             float w[K];
 #pragma unroll
             for (int t = 0; t < K; t++) w[t] = tap[t];
-            for (int task = threadIdx.x; task < ncol * (O8 / OB); task += blockDim.x) {
-                int c = cz_lo + task % ncol, ob = task / ncol;
+            const int nb = b_hi - b_lo;
+            const int ncc = (ncol + 31) >> 5;
+            for (int p = warp; p < ncc * nb; p += nwarp) {
+                const int cc = p % ncc, ob = b_lo + p / ncc;
+                const int c = cz_lo + (cc << 5) + lane;
+                if (c >= cz_hi) continue;
+                const float *sp = S + ob * OB * SC + c;
                 float win[OB + K - 1];
 #pragma unroll
-                for (int i = 0; i < OB + K - 1; i++) win[i] = S[(ob * OB + i) * SC + c];
+                for (int i = 0; i < OB + K - 1; i++) win[i] = sp[i * SC];
+                float *tq = Tt + c * TS + ob * OB;
 #pragma unroll
                 for (int j = 0; j < OB; j++) {
                     float o = 0.f;
 #pragma unroll
                     for (int t = 0; t < K; t++) o = fmaf(w[t], win[j + t], o);
-                    Tt[c * TS + ob * OB + j] = o;
+                    tq[j] = o;
                 }
             }
         }
@@ -135,10 +159,14 @@ __global__ void __launch_bounds__(512, 1)
             for (int t = 0; t < K; t++) w[t] = tap[K + t];
             float *Wp = W + ((size_t)slot * g.Lp + xp) * g.nya * nz;
             const bool amul = Ap && g.att_first;
-            for (int task = threadIdx.x; task < n3; task += blockDim.x) {
-                const int o_row = task % O8, zb = task / O8;
+            // warp-tasks (32-row chunk, z block); lanes take consecutive output rows
+            const int nrc = ((b_hi - b_lo) * OB + 31) >> 5;
+            for (int p = warp; p < nrc * (Z8 / OB); p += nwarp) {
+                const int rc = p % nrc, zb = p / nrc;
+                const int o_row = b_lo * OB + (rc << 5) + lane;
+                if (o_row >= b_hi * OB) continue;
                 const int y = g.pad - H + o_row;
-                const bool store = o_row < NO && y >= g.ya_lo && y < g.ya_hi;
+                const bool store = y >= ra && y <= rb;
                 const int zl0 = zb * OB;
                 const bool full = VEC && (zl0 + OB <= Zc);
                 const size_t rowoff = (size_t)(y - g.ya_lo) * nz + z0 + zl0;
@@ -157,9 +185,10 @@ __global__ void __launch_bounds__(512, 1)
                 }
                 float o[OB];
                 if (g.psf2d) {
+                    const float *tq = Tt + zb * OB * TS + o_row;
                     float win[OB + K - 1];
 #pragma unroll
-                    for (int i = 0; i < OB + K - 1; i++) win[i] = Tt[(zb * OB + i) * TS + o_row];
+                    for (int i = 0; i < OB + K - 1; i++) win[i] = tq[i * TS];
 #pragma unroll
                     for (int j = 0; j < OB; j++) {
                         float s2 = 0.f;
@@ -202,6 +231,7 @@ __global__ void k_b1_nopsf(SpectDev g, const float *__restrict__ proj,
     const int r = i / g.nz, z = i % g.nz;
     const int y = g.ya_lo + r;
     const int ga = alist[slot];
+    if (i == 0) g.wrange[(size_t)slot * g.Lp + xp] = make_int2(0, g.nya);
     float v = 0.f;
     if (y >= g.pad && y < g.pad + g.N) {
         v = proj[((size_t)slot * g.N + (y - g.pad)) * g.nz + z];
@@ -213,23 +243,42 @@ __global__ void k_b1_nopsf(SpectDev g, const float *__restrict__ proj,
 
 template <int K>
 static cudaError_t launch_b1_psf_k(const SpectDev &g, const float *proj, const int *alist,
-                                   int n_slots, int n_chunks, int Zt, float *W, cudaStream_t st) {
+                                   const int4 *items, int n_items, int Zt, float *W,
+                                   cudaStream_t st) {
     size_t smem = b1_psf_smem_bytes(K, g.N, Zt);
-    dim3 grid(n_chunks, n_slots, (g.nz + Zt - 1) / Zt);
-    if (g.nz % 4 == 0)
-        k_b1_psf<K, true><<<grid, 512, smem, st>>>(g, proj, alist, n_chunks, Zt, W);
-    else
-        k_b1_psf<K, false><<<grid, 512, smem, st>>>(g, proj, alist, n_chunks, Zt, W);
+    dim3 grid(n_items, (g.nz + Zt - 1) / Zt);
+    const bool fx = b1_fixed(K, g.N, Zt);
+    if (g.nz % 4 == 0) {
+        if (fx)
+            k_b1_psf<K, true, true><<<grid, 512, smem, st>>>(g, proj, alist, items, Zt, W);
+        else
+            k_b1_psf<K, true, false><<<grid, 512, smem, st>>>(g, proj, alist, items, Zt, W);
+    } else {
+        if (fx)
+            k_b1_psf<K, false, true><<<grid, 512, smem, st>>>(g, proj, alist, items, Zt, W);
+        else
+            k_b1_psf<K, false, false><<<grid, 512, smem, st>>>(g, proj, alist, items, Zt, W);
+    }
     return cudaGetLastError();
 }
 
 template <int K>
 static cudaError_t setup_b1_k(size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_b1_psf<K, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_b1_psf<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_b1_psf<K, true, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(k_b1_psf<K, true, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(k_b1_psf<K, false, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_b1_psf<K, false, false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t setup_b1(int K, size_t smem) {
@@ -244,16 +293,23 @@ cudaError_t setup_b1(int K, size_t smem) {
     }
 }
 
+static bool b1_fixed(int K, int N, int Zt) {
+    int OB = (K <= 31) ? 8 : 4;
+    return N <= 128 && (Zt + OB - 1) / OB * OB <= 128;
+}
+
 size_t b1_psf_smem_bytes(int K, int N, int Zt) {
     int H = K / 2, OB = (K <= 31) ? 8 : 4;
     int O8 = (N + 2 * H + OB - 1) / OB * OB;
     int Z8 = (Zt + OB - 1) / OB * OB;
-    return sizeof(float) *
-           ((size_t)(O8 + 2 * H) * (Z8 + 2 * H) + (size_t)(Z8 + 2 * H) * (O8 + 1) + 4 * K);
+    const bool fx = b1_fixed(K, N, Zt);
+    size_t SC = fx ? 128 + 2 * H : Z8 + 2 * H;
+    size_t TS = fx ? (128 + 2 * H + OB - 1) / OB * OB + 1 : O8 + 1;
+    return sizeof(float) * ((size_t)(O8 + 2 * H) * SC + (size_t)(Z8 + 2 * H) * TS + 4 * K);
 }
 
 cudaError_t launch_b1(const SpectDev &g, const float *proj, const int *alist, int n_slots,
-                      int n_chunks, int Zt, float *W, cudaStream_t st) {
+                      const int4 *items, int n_items, int Zt, float *W, cudaStream_t st) {
     if (!g.psf) {
         dim3 grid((g.nya * g.nz + 255) / 256, g.Lp, n_slots);
         k_b1_nopsf<<<grid, 256, 0, st>>>(g, proj, alist, W);
@@ -262,7 +318,7 @@ cudaError_t launch_b1(const SpectDev &g, const float *proj, const int *alist, in
     switch (g.K) {
 #define GB_B1_CASE(KK) \
     case KK:           \
-        return launch_b1_psf_k<KK>(g, proj, alist, n_slots, n_chunks, Zt, W, st);
+        return launch_b1_psf_k<KK>(g, proj, alist, items, n_items, Zt, W, st);
         GB_FOR_EACH_K(GB_B1_CASE)
 #undef GB_B1_CASE
         default:
@@ -378,8 +434,10 @@ __global__ void __launch_bounds__(256)
         rot_coords(g.theta_bwd + 6 * alist[s + 1], lr, lc, g.half, ix2, iy2);
         Bilin b1 = bilin(ix, iy), b2 = bilin(ix2, iy2);
         float4 v1, v2;
-        sample4(W + s * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b1, z, v1);
-        sample4(W + (s + 1) * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b2, z, v2);
+        sample4_ranged(W + s * slab, g.Lp, g.nya, nz, g.ya_lo, g.wrange + (size_t)s * g.Lp, b1,
+                       z, v1);
+        sample4_ranged(W + (s + 1) * slab, g.Lp, g.nya, nz, g.ya_lo,
+                       g.wrange + (size_t)(s + 1) * g.Lp, b2, z, v2);
         bp.x = __fadd_rn(__fadd_rn(bp.x, v1.x), v2.x);
         bp.y = __fadd_rn(__fadd_rn(bp.y, v1.y), v2.y);
         bp.z = __fadd_rn(__fadd_rn(bp.z, v1.z), v2.z);
@@ -390,7 +448,8 @@ __global__ void __launch_bounds__(256)
         rot_coords(g.theta_bwd + 6 * alist[s], lr, lc, g.half, ix, iy);
         Bilin b1 = bilin(ix, iy);
         float4 v1;
-        sample4(W + s * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b1, z, v1);
+        sample4_ranged(W + s * slab, g.Lp, g.nya, nz, g.ya_lo, g.wrange + (size_t)s * g.Lp, b1,
+                       z, v1);
         bp.x = __fadd_rn(bp.x, v1.x);
         bp.y = __fadd_rn(bp.y, v1.y);
         bp.z = __fadd_rn(bp.z, v1.z);
@@ -420,7 +479,8 @@ __global__ void __launch_bounds__(256)
         rot_coords(th, lr, lc, g.half, ix, iy);
         Bilin b = bilin(ix, iy);
         // W rows = padded x (row offset 0), cols = padded y - ya_lo
-        bp = __fadd_rn(bp, sample(W + s * slab, g.Lp, g.nya, nz, 0, g.ya_lo, b, z));
+        bp = __fadd_rn(bp, sample_ranged(W + s * slab, g.Lp, g.nya, nz, g.ya_lo,
+                                         g.wrange + (size_t)s * g.Lp, b, z));
     }
     const size_t i = ((size_t)x * N + y) * nz + z;
     apply_update(mode, u, i, x, y, z, N, N, nz, bp, out);
@@ -450,6 +510,8 @@ __global__ void __launch_bounds__(256)
     if (i >= g.nya * g.nz) return;
     const int r = i / g.nz, z = i % g.nz;
     const int yp = g.ya_lo + r;
+    const int2 rg = g.wrange[(size_t)slot * g.Lp + xp];
+    if (r < rg.x || r >= rg.y) return;
     const float v = W[(((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z];
     if (v == 0.f) return;
     const float *th = g.theta_fwd + 6 * alist[slot];

@@ -17,6 +17,23 @@
 
 namespace gb {
 
+#ifdef GB_PHASE_TIMING
+// Per-CTA cycle counts of the forward kernel's phases (diagnostic builds only):
+// [0] waits for the attenuation copy, [1] phase 1, [2] phase 2, [3] phase 3,
+// [4] planes processed, [5] total.
+__device__ unsigned long long g_fwd_phase_cycles[4096 * 8];
+#define GB_T(k, v)                                              \
+    do {                                                        \
+        if (threadIdx.x == 0) tacc[k] += (v);                   \
+    } while (0)
+#define GB_NOW() clock64()
+#else
+#define GB_T(k, v) \
+    do {           \
+    } while (0)
+#define GB_NOW() 0LL
+#endif
+
 // Does the sample segment of plane xp (rows y in [ya, yb]) touch the object square
 // [pad-1, pad+N] x [pad-1, pad+N] in padded coordinates?  Liang-Barsky clip.
 __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, int xp, int ya,
@@ -45,30 +62,39 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 // Shared-memory layout (per CTA):
 //   S  [SR][SC]: rotated, attenuated samples; row r <-> padded y = pad - H + r,
 //                column c <-> z = z0 - HP + c  (HP = H rounded up to 4: 16-byte aligned
-//                z quads)
+//                z quads).  Before phase 1 of a plane, the attenuation rows of that
+//                plane are bulk-copied (TMA) into S and multiplied in place.
 //   Tt [TR][TS]: y-blurred plane, transposed; row c <-> z = z0 - HP + c, column = output y
 //   taps [2][2][K]: double-buffered y / z taps of the current plane
-template <int K, bool VEC>
+//   one mbarrier for the TMA copies
+// Per plane only the rows the rotated object square can reach are sampled / blurred.
+// FIXED: the tile fits 128 output rows and a 128-wide z slab, so the shared-memory row
+// strides are compile-time constants (immediate-offset loads in the blur loops).
+template <int K, bool VEC, bool FIXED>
 __global__ void __launch_bounds__(512, 1)
     k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
-              int n_chunks, int Zt, float *__restrict__ partials) {
+              const int4 *__restrict__ items, int Zt, float *__restrict__ partials) {
     constexpr int H = K / 2;
     constexpr int HP = (H + 3) / 4 * 4;
     constexpr int OB = (K <= 31) ? 8 : 4;  // outputs per task
     constexpr int NACC = 32 / OB;          // phase-3 tasks per thread
-    const int slot = blockIdx.y, chunk = blockIdx.x;
+    const int4 item = items[blockIdx.x];  // (slot, first plane, end plane)
+    const int slot = item.x;
     const int ga = alist[slot];
     const int N = g.N, nz = g.nz;
-    const int z0 = blockIdx.z * Zt;
+    const int z0 = blockIdx.y * Zt;
     const int Zc = min(Zt, nz - z0);
     const int N8 = (N + OB - 1) / OB * OB;
     const int Z8 = (Zc + OB - 1) / OB * OB;
-    const int SC = Z8 + 2 * HP, SR = N8 + 2 * H;
-    const int TS = N8 + 1, TR = Z8 + 2 * HP;
-    extern __shared__ __align__(16) float sm[];
+    constexpr int SC_FIX = 128 + 2 * HP, TS_FIX = 129;
+    const int SC = FIXED ? SC_FIX : Z8 + 2 * HP, SR = N8 + 2 * H;
+    const int TS = FIXED ? TS_FIX : N8 + 1, TR = Z8 + 2 * HP;
+    extern __shared__ __align__(128) float sm[];
     float *S = sm;
     float *Tt = S + SR * SC;
     float *tp = Tt + TR * TS;
+    unsigned long long *bar =
+        reinterpret_cast<unsigned long long *>(tp + ((4 * K + 1) & ~1));
     for (int i = threadIdx.x; i < SR * SC + TR * TS; i += blockDim.x) sm[i] = 0.f;
 
     float th[6];
@@ -76,26 +102,63 @@ __global__ void __launch_bounds__(512, 1)
     for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * ga + k];
     const int grp = g.group[ga];
     const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
-    const int x0 = chunk * g.Lp / n_chunks, x1 = (chunk + 1) * g.Lp / n_chunks;
+    const bool amul = A && g.att_first;
+    const bool use_tma = VEC && amul;
+    const int x0 = item.y, x1 = item.z;
     const int zv_lo = max(0, z0 - H), zv_hi = min(nz, z0 + Zc + H);  // z needed by the blur
     const int cz_lo = zv_lo - z0 + HP, cz_hi = zv_hi - z0 + HP;
     const int ncol = cz_hi - cz_lo;
     const int ylo = max(0, g.pad - H), yhi = min(g.Lp, g.pad + N + H);  // sampled rows
-    const int n3 = N8 * (Z8 / OB);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-    // z quads covering [zv_lo, zv_hi) (vector path)
-    const int zq_lo = zv_lo & ~3, zq_hi = (zv_hi + 3) & ~3;
+    const int zq_lo = zv_lo & ~3, zq_hi = (zv_hi + 3) & ~3;  // z quads (vector path)
     const int nq = (zq_hi - zq_lo) >> 2;
+    const unsigned row_bytes = (unsigned)(zq_hi - zq_lo) * 4u;
+    const int qcol0 = zq_lo - z0 + HP;  // S column of the first quad
+    if (threadIdx.x == 0 && use_tma) mbar_init(bar, 1);
     float acc[NACC][OB];
+    int ty[NACC], tz[NACC];  // phase-3 task (output row, z block) of this thread
 #pragma unroll
-    for (int k = 0; k < NACC; k++)
+    for (int k = 0; k < NACC; k++) {
+        const int task = threadIdx.x + k * blockDim.x;
+        ty[k] = task % N8;
+        tz[k] = task / N8;
 #pragma unroll
         for (int j = 0; j < OB; j++) acc[k][j] = 0.f;
+    }
     __syncthreads();
 
+    // next plane with any sample on the object, from xp on; rows in [ra, rb]
+    auto next_plane = [&](int xp, int &ra, int &rb) {
+        for (; xp < x1; ++xp)
+            if (plane_rows(g, th, xp, ylo, yhi, 0.5f, ra, rb)) return xp;
+        return x1;
+    };
+    // bulk-copy the attenuation rows [ra, rb] of plane xp into S (warp 0)
+    auto issue_tma = [&](int xp, int ra, int rb) {
+        if (warp != 0) return;
+        if (lane == 0) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(bar, row_bytes * (unsigned)(rb - ra + 1));
+        }
+        __syncwarp();
+        const float *src = A + ((size_t)xp * g.nya + (ra - g.ya_lo)) * nz + zq_lo;
+        for (int y = ra + lane; y <= rb; y += 32)
+            tma_load_1d(S + (y - (g.pad - H)) * SC + qcol0, src + (size_t)(y - ra) * nz,
+                        row_bytes, bar);
+    };
+
+    int ra = 0, rb = -1, pra = 0, prb = -1;  // current and previous sampled rows
+    int xp = next_plane(x0, ra, rb);
+    if (use_tma && xp < x1) issue_tma(xp, ra, rb);
     int parity = 0;
-    for (int xp = x0; xp < x1; ++xp) {
-        if (!plane_hits(g, th, xp, ylo, yhi - 1)) continue;
+    unsigned phase = 0;
+#ifdef GB_PHASE_TIMING
+    unsigned long long tacc[6] = {0, 0, 0, 0, 0, 0};
+    const long long t_start = clock64();
+#endif
+    long long t0 = GB_NOW();
+    while (xp < x1) {
+        t0 = GB_NOW();
         const float lr = g.lin[xp];
         float *tap = tp + parity * 2 * K;
         if (threadIdx.x < K) {
@@ -103,90 +166,149 @@ __global__ void __launch_bounds__(512, 1)
             tap[K + threadIdx.x] =
                 g.psf2d ? g.taps_z[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x] : 0.f;
         }
-        // phase 1: rotated samples (times A when attenuation precedes the PSF)
+        if (use_tma) {
+            const bool ok = mbar_wait_bounded(bar, phase, 1u << 22);
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0 && g.err) atomicExch(g.err, GB_ERR_WAIT_TIMEOUT);
+                return;
+            }
+            phase ^= 1u;
+        }
+        {
+            long long t1 = GB_NOW();
+            GB_T(0, t1 - t0);
+            t0 = t1;
+        }
+        // phase 1: rotated samples of rows [ra, rb] (times A when attenuation precedes
+        // the PSF); stale rows of the previous plane are cleared
         const float *Ap = A ? A + (size_t)xp * g.nya * nz : nullptr;
-        const bool amul = Ap && g.att_first;
         if (VEC) {
-            // one row per warp, two rows in flight, z quads across lanes
-            for (int y = ylo + warp; y < yhi; y += 2 * nwarp) {
-                const int y2 = y + nwarp;
-                const bool two = y2 < yhi;
-                float ix, iy, ix2, iy2;
-                rot_coords(th, lr, g.lin[y], g.half, ix, iy);
-                rot_coords(th, lr, g.lin[two ? y2 : y], g.half, ix2, iy2);
-                const Bilin b1 = bilin(ix, iy), b2 = bilin(ix2, iy2);
-                float *S1 = S + (y - (g.pad - H)) * SC;
-                float *S2 = S + (y2 - (g.pad - H)) * SC;
+            for (int y = pra + warp; y <= prb; y += nwarp) {
+                if (y >= ra && y <= rb) continue;
+                float *Sr = S + (y - (g.pad - H)) * SC + qcol0;
+                for (int q = lane; q < nq; q += 32)
+                    *reinterpret_cast<float4 *>(Sr + 4 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            for (int y0 = ra + warp; y0 <= rb; y0 += 4 * nwarp) {
+                int ys[4];
+                bool okr[4];
+                Bilin b[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    ys[u] = y0 + u * nwarp;
+                    okr[u] = ys[u] <= rb;
+                    float ix, iy;
+                    rot_coords(th, lr, g.lin[okr[u] ? ys[u] : y0], g.half, ix, iy);
+                    b[u] = bilin(ix, iy);
+                }
                 for (int q = lane; q < nq; q += 32) {
                     const int z = zq_lo + 4 * q;
-                    float4 v1, v2;
-                    bool h1 = sample4(f, N, N, nz, g.pad, g.pad, b1, z, v1);
-                    bool h2 = two && sample4(f, N, N, nz, g.pad, g.pad, b2, z, v2);
-                    if (amul && h1)
-                        v1 = mul4(v1, __ldg(reinterpret_cast<const float4 *>(
-                                          Ap + (size_t)(y - g.ya_lo) * nz + z)));
-                    if (amul && h2)
-                        v2 = mul4(v2, __ldg(reinterpret_cast<const float4 *>(
-                                          Ap + (size_t)(y2 - g.ya_lo) * nz + z)));
-                    *reinterpret_cast<float4 *>(S1 + (z - z0 + HP)) = v1;
-                    if (two) *reinterpret_cast<float4 *>(S2 + (z - z0 + HP)) = h2 ? v2 : make_float4(0.f, 0.f, 0.f, 0.f);
+                    float4 v[4];
+                    bool h[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+                        h[u] = okr[u] && sample4(f, N, N, nz, g.pad, g.pad, b[u], z, v[u]);
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        if (!okr[u]) continue;
+                        float4 *dst = reinterpret_cast<float4 *>(
+                            S + (ys[u] - (g.pad - H)) * SC + qcol0 + 4 * q);
+                        float4 o = v[u];
+                        if (amul) {
+                            float4 a = use_tma ? *dst
+                                               : (h[u] ? __ldg(reinterpret_cast<const float4 *>(
+                                                             Ap + (size_t)(ys[u] - g.ya_lo) * nz + z))
+                                                       : make_float4(0.f, 0.f, 0.f, 0.f));
+                            o = mul4(o, a);
+                        }
+                        *dst = h[u] ? o : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
                 }
             }
         } else {
             for (int i = threadIdx.x; i < (yhi - ylo) * ncol; i += blockDim.x) {
                 int y = ylo + i / ncol, c = cz_lo + i % ncol;
                 int z = z0 - HP + c;
-                float ix, iy;
-                rot_coords(th, lr, g.lin[y], g.half, ix, iy);
-                Bilin b = bilin(ix, iy);
-                float v = sample(f, N, N, nz, g.pad, g.pad, b, z);
-                if (amul && v != 0.f) v = __fmul_rn(v, Ap[(size_t)(y - g.ya_lo) * nz + z]);
+                float v = 0.f;
+                if (y >= ra && y <= rb) {
+                    float ix, iy;
+                    rot_coords(th, lr, g.lin[y], g.half, ix, iy);
+                    Bilin bb = bilin(ix, iy);
+                    v = sample(f, N, N, nz, g.pad, g.pad, bb, z);
+                    if (amul && v != 0.f) v = __fmul_rn(v, Ap[(size_t)(y - g.ya_lo) * nz + z]);
+                }
                 S[(y - (g.pad - H)) * SC + c] = v;
             }
         }
         __syncthreads();
-        // phase 2: blur along y, write transposed
+        {
+            long long t1 = GB_NOW();
+            GB_T(1, t1 - t0);
+            t0 = t1;
+        }
+        // output rows (local y in [0, N)) that the blurred plane can reach
+        const int o_lo = max(0, ra - H - g.pad), o_hi = min(N, rb + H - g.pad + 1);
+        const int b_lo = o_lo / OB, b_hi = (o_hi + OB - 1) / OB;
+        // phase 2: blur along y, write transposed.  Warp-tasks are (32-column chunk, row
+        // block); lanes take consecutive columns.
         {
             float w[K];
 #pragma unroll
             for (int t = 0; t < K; t++) w[t] = tap[t];
-            for (int task = threadIdx.x; task < ncol * (N8 / OB); task += blockDim.x) {
-                int c = cz_lo + task % ncol, yb = task / ncol;
+            const int nb = b_hi - b_lo;
+            const int ncc = (ncol + 31) >> 5;
+            for (int p = warp; p < ncc * nb; p += nwarp) {
+                const int cc = p % ncc, yb = b_lo + p / ncc;
+                const int c = cz_lo + (cc << 5) + lane;
+                if (c >= cz_hi) continue;
+                const float *sp = S + yb * OB * SC + c;
                 float win[OB + K - 1];
 #pragma unroll
-                for (int i = 0; i < OB + K - 1; i++) win[i] = S[(yb * OB + i) * SC + c];
+                for (int i = 0; i < OB + K - 1; i++) win[i] = sp[i * SC];
+                float *tq = Tt + c * TS + yb * OB;
 #pragma unroll
                 for (int j = 0; j < OB; j++) {
                     float o = 0.f;
 #pragma unroll
                     for (int t = 0; t < K; t++) o = fmaf(w[t], win[j + t], o);
-                    Tt[c * TS + yb * OB + j] = o;
+                    tq[j] = o;
                 }
             }
         }
         __syncthreads();
+        {
+            long long t1 = GB_NOW();
+            GB_T(2, t1 - t0);
+            t0 = t1;
+        }
+        // S is free until the next phase 1: start the next plane's attenuation copy
+        pra = ra;
+        prb = rb;
+        int nra = 0, nrb = -1;
+        const int nxp = next_plane(xp + 1, nra, nrb);
+        if (use_tma && nxp < x1) issue_tma(nxp, nra, nrb);
         // phase 3: blur along z (2D PSF), optional attenuation after the PSF, accumulate
         {
             float w[K];
 #pragma unroll
             for (int t = 0; t < K; t++) w[t] = tap[K + t];
+            const int y_lo = b_lo * OB, y_hi = b_hi * OB;
 #pragma unroll
             for (int k = 0; k < NACC; k++) {
-                int task = threadIdx.x + k * blockDim.x;
-                if (task < n3) {
-                    int y = task % N8, zb = task / N8;
+                const int y = ty[k], zb = tz[k];
+                if (zb * OB < Z8 && y >= y_lo && y < y_hi) {
                     float o[OB];
                     if (g.psf2d) {
+                        const float *tq = Tt + (zb * OB + HP - H) * TS + y;
                         float win[OB + K - 1];
 #pragma unroll
-                        for (int i = 0; i < OB + K - 1; i++)
-                            win[i] = Tt[(zb * OB + i + HP - H) * TS + y];
+                        for (int i = 0; i < OB + K - 1; i++) win[i] = tq[i * TS];
 #pragma unroll
                         for (int j = 0; j < OB; j++) {
-                            float s = 0.f;
+                            float s2 = 0.f;
 #pragma unroll
-                            for (int t = 0; t < K; t++) s = fmaf(w[t], win[j + t], s);
-                            o[j] = s;
+                            for (int t = 0; t < K; t++) s2 = fmaf(w[t], win[j + t], s2);
+                            o[j] = s2;
                         }
                     } else {
 #pragma unroll
@@ -206,35 +328,46 @@ __global__ void __launch_bounds__(512, 1)
                 }
             }
         }
+        {
+            long long t1 = GB_NOW();
+            GB_T(3, t1 - t0);
+            GB_T(4, 1);
+        }
         parity ^= 1;
+        xp = nxp;
+        ra = nra;
+        rb = nrb;
     }
-    // partial ray sums of this chunk
-    float *out = partials + ((size_t)slot * n_chunks + chunk) * N * nz;
+#ifdef GB_PHASE_TIMING
+    if (threadIdx.x == 0 && blockIdx.x < 4096) {
+        tacc[5] = clock64() - t_start;
+        for (int k = 0; k < 6; k++) g_fwd_phase_cycles[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
+    }
+#endif
+    // partial ray sums of this item
+    float *out = partials + (size_t)blockIdx.x * N * nz;
 #pragma unroll
     for (int k = 0; k < NACC; k++) {
-        int task = threadIdx.x + k * blockDim.x;
-        if (task < n3) {
-            int y = task % N8, zb = task / N8;
-            if (y < N) {
+        const int y = ty[k], zb = tz[k];
+        if (zb * OB < Z8 && y < N) {
 #pragma unroll
-                for (int j = 0; j < OB; j++) {
-                    int z = z0 + zb * OB + j;
-                    if (z - z0 < Zc) out[(size_t)y * nz + z] = acc[k][j];
-                }
+            for (int j = 0; j < OB; j++) {
+                int z = z0 + zb * OB + j;
+                if (z - z0 < Zc) out[(size_t)y * nz + z] = acc[k][j];
             }
         }
     }
 }
 
 // ------------------------------------------------------------- without PSF
-// One thread per output (y, z) of a chunk of planes; A read on the fly.
+// One thread per output (y, z) of an item's planes; A read on the fly.
 __global__ void __launch_bounds__(256)
     k_fwd_nopsf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
-                int n_chunks, float *__restrict__ partials) {
-    const int slot = blockIdx.y, chunk = blockIdx.x;
-    const int ga = alist[slot];
+                const int4 *__restrict__ items, float *__restrict__ partials) {
+    const int4 item = items[blockIdx.x];
+    const int ga = alist[item.x];
     const int N = g.N, nz = g.nz;
-    const int i = blockIdx.z * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.x + threadIdx.x;
     if (i >= N * nz) return;
     const int y = i / nz, z = i % nz;
     float th[6];
@@ -243,9 +376,8 @@ __global__ void __launch_bounds__(256)
     const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
     const int yp = g.pad + y;
     const float lc = g.lin[yp];
-    const int x0 = chunk * g.Lp / n_chunks, x1 = (chunk + 1) * g.Lp / n_chunks;
     float acc = 0.f;
-    for (int xp = x0; xp < x1; ++xp) {
+    for (int xp = item.y; xp < item.z; ++xp) {
         float ix, iy;
         rot_coords(th, g.lin[xp], lc, g.half, ix, iy);
         Bilin b = bilin(ix, iy);
@@ -253,22 +385,22 @@ __global__ void __launch_bounds__(256)
         if (A) v = __fmul_rn(v, __ldg(A + ((size_t)xp * g.nya + (yp - g.ya_lo)) * nz + z));
         acc += v;
     }
-    partials[((size_t)slot * n_chunks + chunk) * N * nz + i] = acc;
+    partials[(size_t)blockIdx.x * N * nz + i] = acc;
 }
 
 // --------------------------------------------------------------- reduction
-// out[slot][i] = sum_c partials[slot][c][i] in chunk order.  With `ratio`,
-// out = g[ga][i] / (sum + s[ga][i] + delta) and pred (optional) = sum + s.
-__global__ void k_reduce(int n_chunks, int NZ, const float *__restrict__ partials,
+// out[slot][i] = sum of the partials of the slot's items, in item order.  With
+// `ratio`, out = g[ga][i] / (sum + s[ga][i] + delta) and pred (optional) = sum + s.
+__global__ void k_reduce(const int *__restrict__ ioff, int NZ, const float *__restrict__ partials,
                          float *__restrict__ out, int ratio, const float *__restrict__ gproj,
                          const float *__restrict__ sadd, const int *__restrict__ alist,
                          float *__restrict__ pred) {
     const int slot = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= NZ) return;
-    const float *p = partials + (size_t)slot * n_chunks * NZ + i;
+    const int c0 = ioff[slot], c1 = ioff[slot + 1];
     float v = 0.f;
-    for (int c = 0; c < n_chunks; c++) v += p[(size_t)c * NZ];
+    for (int c = c0; c < c1; c++) v += partials[(size_t)c * NZ + i];
     size_t o = (size_t)slot * NZ + i;
     if (!ratio) {
         out[o] = v;
@@ -282,34 +414,60 @@ __global__ void k_reduce(int n_chunks, int NZ, const float *__restrict__ partial
 }
 
 // ------------------------------------------------------------- launchers
+static bool fwd_fixed(int K, int N, int Zt) {
+    int OB = (K <= 31) ? 8 : 4;
+    return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= 128;
+}
+
 size_t fwd_psf_smem_bytes(int K, int N, int Zt) {
     int H = K / 2, HP = (H + 3) / 4 * 4, OB = (K <= 31) ? 8 : 4;
     int N8 = (N + OB - 1) / OB * OB;
     int Z8 = (Zt + OB - 1) / OB * OB;
-    return sizeof(float) *
-           ((size_t)(N8 + 2 * H) * (Z8 + 2 * HP) + (size_t)(Z8 + 2 * HP) * (N8 + 1) + 4 * K);
+    const bool fx = fwd_fixed(K, N, Zt);
+    size_t SC = fx ? 128 + 2 * HP : Z8 + 2 * HP, TS = fx ? 129 : N8 + 1;
+    return sizeof(float) * ((size_t)(N8 + 2 * H) * SC + (size_t)(Z8 + 2 * HP) * TS +
+                            ((4 * K + 1) & ~1)) +
+           sizeof(unsigned long long);
 }
 
 template <int K>
 static cudaError_t launch_fwd_psf_k(const SpectDev &g, const float *f, const int *alist,
-                                    int n_slots, int n_chunks, int Zt, float *partials,
+                                    const int4 *items, int n_items, int Zt, float *partials,
                                     cudaStream_t st) {
     size_t smem = fwd_psf_smem_bytes(K, g.N, Zt);
-    dim3 grid(n_chunks, n_slots, (g.nz + Zt - 1) / Zt);
-    if (g.nz % 4 == 0)
-        k_fwd_psf<K, true><<<grid, 512, smem, st>>>(g, f, alist, n_chunks, Zt, partials);
-    else
-        k_fwd_psf<K, false><<<grid, 512, smem, st>>>(g, f, alist, n_chunks, Zt, partials);
+    dim3 grid(n_items, (g.nz + Zt - 1) / Zt);
+    const bool fx = fwd_fixed(K, g.N, Zt);
+    if (g.nz % 4 == 0) {
+        if (fx)
+            k_fwd_psf<K, true, true><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+        else
+            k_fwd_psf<K, true, false><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+    } else {
+        if (fx)
+            k_fwd_psf<K, false, true><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+        else
+            k_fwd_psf<K, false, false><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+    }
     return cudaGetLastError();
 }
 
 template <int K>
 static cudaError_t setup_fwd_k(size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_fwd_psf<K, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_fwd_psf<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_fwd_psf<K, true, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(k_fwd_psf<K, true, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(k_fwd_psf<K, false, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    return cudaFuncSetAttribute(k_fwd_psf<K, false, false>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t setup_fwd(int K, size_t smem) {
@@ -324,17 +482,17 @@ cudaError_t setup_fwd(int K, size_t smem) {
     }
 }
 
-cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, int n_slots,
-                       int n_chunks, int Zt, float *partials, cudaStream_t st) {
+cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, const int4 *items,
+                       int n_items, int Zt, float *partials, cudaStream_t st) {
     if (!g.psf) {
-        dim3 grid(n_chunks, n_slots, (g.N * g.nz + 255) / 256);
-        k_fwd_nopsf<<<grid, 256, 0, st>>>(g, f, alist, n_chunks, partials);
+        dim3 grid(n_items, (g.N * g.nz + 255) / 256);
+        k_fwd_nopsf<<<grid, 256, 0, st>>>(g, f, alist, items, partials);
         return cudaGetLastError();
     }
     switch (g.K) {
 #define GB_FWD_CASE(KK) \
     case KK:            \
-        return launch_fwd_psf_k<KK>(g, f, alist, n_slots, n_chunks, Zt, partials, st);
+        return launch_fwd_psf_k<KK>(g, f, alist, items, n_items, Zt, partials, st);
         GB_FOR_EACH_K(GB_FWD_CASE)
 #undef GB_FWD_CASE
         default:
@@ -342,11 +500,18 @@ cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, int 
     }
 }
 
-cudaError_t launch_reduce(int n_slots, int n_chunks, int NZ, const float *partials, float *out,
+#ifdef GB_PHASE_TIMING
+extern "C" int gb_debug_fwd_phase_cycles(unsigned long long *out, int n) {
+    return (int)cudaMemcpyFromSymbol(out, g_fwd_phase_cycles,
+                                     sizeof(unsigned long long) * (size_t)n);
+}
+#endif
+
+cudaError_t launch_reduce(int n_slots, const int *ioff, int NZ, const float *partials, float *out,
                           int ratio, const float *gproj, const float *sadd, const int *alist,
                           float *pred, cudaStream_t st) {
     dim3 grid((NZ + 255) / 256, n_slots);
-    k_reduce<<<grid, 256, 0, st>>>(n_chunks, NZ, partials, out, ratio, gproj, sadd, alist, pred);
+    k_reduce<<<grid, 256, 0, st>>>(ioff, NZ, partials, out, ratio, gproj, sadd, alist, pred);
     return cudaGetLastError();
 }
 

@@ -23,6 +23,8 @@ namespace gb {
 constexpr float kDelta = 1e-11f;  // pytomography.delta (src/pytomography/__init__.py:21)
 
 struct SpectDev {
+    int *err;               // device error word (bounded waits that gave up), or null
+    int2 *wrange;           // [G][Lp] W column range written per (slot, plane), or null
     int N, nz, pad, Lp;
     int ya_lo, ya_hi, nya;  // stored row range of A and W
     float half;             // (Lp - 1) / 2
@@ -90,11 +92,11 @@ __device__ __forceinline__ Bilin bilin(float ix, float iy) {
     return b;
 }
 
+// ((vnw*nw + vne*ne) + vsw*sw) + vse*se, the grid_sample summation order, with fused
+// multiply-adds (rounding differs from the unfused CPU order by at most an ulp or two).
 __device__ __forceinline__ float bilin_combine(const Bilin &b, float vnw, float vne, float vsw,
                                                float vse) {
-    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(vnw, b.nw), __fmul_rn(vne, b.ne)),
-                               __fmul_rn(vsw, b.sw)),
-                     __fmul_rn(vse, b.se));
+    return fmaf(vse, b.se, fmaf(vsw, b.sw, fmaf(vne, b.ne, vnw * b.nw)));
 }
 
 // Bilinear sample of a [rows][cols][nz] array whose (row, col) origin is shifted by
@@ -137,6 +139,136 @@ __device__ __forceinline__ bool sample4(const float *__restrict__ src, int rows,
     out.w = bilin_combine(b, vnw.w, vne.w, vsw.w, vse.w);
     return true;
 }
+
+// Same as sample4 for the back-projection stack W of one angle slot: plane r holds data
+// only in columns [wr[r].x, wr[r].y); everything else reads as zero.
+__device__ __forceinline__ bool sample4_ranged(const float *__restrict__ src, int rows, int cols,
+                                               int nz, int col_off, const int2 *__restrict__ wr,
+                                               const Bilin &b, int z, float4 &out) {
+    int r = b.r0, c = b.c0 - col_off;
+    out = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool r0 = (unsigned)r < (unsigned)rows, r1 = (unsigned)(r + 1) < (unsigned)rows;
+    int2 g0 = r0 ? wr[r] : make_int2(0, 0);
+    int2 g1 = r1 ? wr[r + 1] : make_int2(0, 0);
+    bool a00 = r0 && c >= g0.x && c < g0.y, a01 = r0 && c + 1 >= g0.x && c + 1 < g0.y;
+    bool a10 = r1 && c >= g1.x && c < g1.y, a11 = r1 && c + 1 >= g1.x && c + 1 < g1.y;
+    if (!(a00 || a01 || a10 || a11)) return false;
+    const float *p = src + ((long long)r * cols + c) * nz + z;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 vnw = a00 ? __ldg(reinterpret_cast<const float4 *>(p)) : zero;
+    float4 vne = a01 ? __ldg(reinterpret_cast<const float4 *>(p + nz)) : zero;
+    float4 vsw = a10 ? __ldg(reinterpret_cast<const float4 *>(p + (long long)cols * nz)) : zero;
+    float4 vse = a11 ? __ldg(reinterpret_cast<const float4 *>(p + (long long)cols * nz + nz)) : zero;
+    out.x = bilin_combine(b, vnw.x, vne.x, vsw.x, vse.x);
+    out.y = bilin_combine(b, vnw.y, vne.y, vsw.y, vse.y);
+    out.z = bilin_combine(b, vnw.z, vne.z, vsw.z, vse.z);
+    out.w = bilin_combine(b, vnw.w, vne.w, vsw.w, vse.w);
+    return true;
+}
+
+__device__ __forceinline__ float sample_ranged(const float *__restrict__ src, int rows, int cols,
+                                               int nz, int col_off, const int2 *__restrict__ wr,
+                                               const Bilin &b, int z) {
+    int r = b.r0, c = b.c0 - col_off;
+    bool r0 = (unsigned)r < (unsigned)rows, r1 = (unsigned)(r + 1) < (unsigned)rows;
+    int2 g0 = r0 ? wr[r] : make_int2(0, 0);
+    int2 g1 = r1 ? wr[r + 1] : make_int2(0, 0);
+    bool a00 = r0 && c >= g0.x && c < g0.y, a01 = r0 && c + 1 >= g0.x && c + 1 < g0.y;
+    bool a10 = r1 && c >= g1.x && c < g1.y, a11 = r1 && c + 1 >= g1.x && c + 1 < g1.y;
+    if (!(a00 || a01 || a10 || a11)) return 0.f;
+    const float *p = src + ((long long)r * cols + c) * nz + z;
+    float vnw = a00 ? __ldg(p) : 0.f;
+    float vne = a01 ? __ldg(p + nz) : 0.f;
+    float vsw = a10 ? __ldg(p + (long long)cols * nz) : 0.f;
+    float vse = a11 ? __ldg(p + (long long)cols * nz + nz) : 0.f;
+    return bilin_combine(b, vnw, vne, vsw, vse);
+}
+
+// Rows y in [ylo, yhi) of plane xp whose sample (rotation th) can land within `margin`
+// pixels of the object square [pad, pad+N) (Liang-Barsky clip of the sample segment,
+// one row of slack on each side).  False when the plane misses the square.
+__device__ __forceinline__ bool plane_rows(const SpectDev &g, const float *th, int xp, int ylo,
+                                           int yhi, float margin, int &ra, int &rb) {
+    const int y0 = ylo, y1 = yhi - 1;
+    float ixa, iya, ixb, iyb;
+    rot_coords(th, g.lin[xp], g.lin[y0], g.half, ixa, iya);
+    rot_coords(th, g.lin[xp], g.lin[y1], g.half, ixb, iyb);
+    const float lo = (float)g.pad - 1.f - margin, hi = (float)(g.pad + g.N) + margin;
+    float t0 = 0.f, t1 = 1.f;
+    const float p[2] = {ixa, iya}, d[2] = {ixb - ixa, iyb - iya};
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        if (fabsf(d[k]) < 1e-12f) {
+            if (p[k] < lo || p[k] > hi) return false;
+        } else {
+            float ta = (lo - p[k]) / d[k], tb = (hi - p[k]) / d[k];
+            if (ta > tb) {
+                float t = ta;
+                ta = tb;
+                tb = t;
+            }
+            t0 = fmaxf(t0, ta);
+            t1 = fminf(t1, tb);
+        }
+    }
+    if (t0 > t1) return false;
+    const float fa = y0 + t0 * (float)(y1 - y0), fb = y0 + t1 * (float)(y1 - y0);
+    ra = max(ylo, (int)floorf(fa) - 1);
+    rb = min(yhi - 1, (int)ceilf(fb) + 1);
+    return ra <= rb;
+}
+
+// ---------------------------------------------------------------- TMA / mbarrier
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Orders this thread's (and, after a CTA barrier, the CTA's) generic-proxy shared-memory
+// accesses before subsequent async-proxy (TMA) writes.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 1-D TMA bulk copy global -> shared, completion counted on `bar` (16-byte aligned
+// addresses, size a multiple of 16).
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes,
+                                            unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Wait for phase `parity` of `bar`, giving up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity,
+                                                  unsigned limit) {
+    for (unsigned i = 0; i < limit; i++) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+constexpr int GB_ERR_WAIT_TIMEOUT = 1;  // value written to SpectDev::err
 
 __device__ __forceinline__ float4 mul4(float4 a, float4 b) {
     return make_float4(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z),

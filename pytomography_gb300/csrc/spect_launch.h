@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "gbtomo.h"
 #include "spect_kernels.cuh"
 
 // PSF tap-count buckets compiled into the library: a plan's taps are zero-padded
@@ -24,13 +25,16 @@ size_t b1_psf_smem_bytes(int K, int N, int Zt);
 cudaError_t setup_fwd(int K, size_t smem);
 cudaError_t setup_b1(int K, size_t smem);
 
-cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, int n_slots,
-                       int n_chunks, int Zt, float *partials, cudaStream_t st);
-cudaError_t launch_reduce(int n_slots, int n_chunks, int NZ, const float *partials, float *out,
+// Work items (int4: slot, first plane, end plane, unused) split each angle's planes
+// into ranges of about equal work; partial sums are indexed by item.
+cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, const int4 *items,
+                       int n_items, int Zt, float *partials, cudaStream_t st);
+// ioff[slot] .. ioff[slot+1]: the items of a slot
+cudaError_t launch_reduce(int n_slots, const int *ioff, int NZ, const float *partials, float *out,
                           int ratio, const float *gproj, const float *sadd, const int *alist,
                           float *pred, cudaStream_t st);
 cudaError_t launch_b1(const SpectDev &g, const float *proj, const int *alist, int n_slots,
-                      int n_chunks, int Zt, float *W, cudaStream_t st);
+                      const int4 *items, int n_items, int Zt, float *W, cudaStream_t st);
 cudaError_t launch_b2_gather(const SpectDev &g, const float *W, const int *alist, int n_slots,
                              float *out, int mode, const UpdateArgs &u, cudaStream_t st);
 cudaError_t launch_b2_scatter(const SpectDev &g, const float *W, const int *alist, int n_slots,
@@ -39,5 +43,18 @@ cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_ang
                          cudaStream_t st);
 cudaError_t launch_rdp(const float *f, float *grad, int nx, int ny, int nz, const UpdateArgs &u,
                        float beta_scale, cudaStream_t st);
+
+// Launch geometry of one forward projection of a plan (for entry points defined outside
+// spect_plan.cu): false when the subset is out of range.
+struct FwdArgs {
+    SpectDev g;
+    const int *alist;
+    int n_sel;
+    const int4 *items;
+    int n_items;
+    const int *ioff;
+    int Zt;
+};
+bool plan_forward_args(const gb_spect_plan *p, int subset, FwdArgs *a);
 
 }  // namespace gb

@@ -51,16 +51,27 @@ struct gb_spect_plan {
     float *d_lin = nullptr, *d_theta_fwd = nullptr, *d_theta_bwd = nullptr;
     float *d_taps_r = nullptr, *d_taps_z = nullptr, *d_A = nullptr;
     int *d_group = nullptr;
-    // angle lists: [all][subset 0][subset 1]...
+    // angle lists: [all][subset 0][subset 1]..., with their work items
     int *d_alist = nullptr;
+    int4 *d_items = nullptr;
+    int *d_ioff = nullptr;
     int n_subsets = 0;
-    std::vector<int> list_off, list_len;
+    struct List {
+        int alist_off = 0, n = 0;
+        int fitem_off = 0, n_fitems = 0;  // forward items in d_items
+        int ioff_off = 0;                 // n + 1 item offsets per slot in d_ioff
+        std::vector<int> gitem_off, n_gitems;  // B1 items of each angle group
+    };
+    std::vector<List> lists;
+    std::vector<float> h_theta_fwd, h_lin;
     // scratch
     float *d_partials = nullptr;
     size_t partials_cap = 0;
     float *d_W = nullptr;
     int G = 0;
     float *d_ratio = nullptr, *d_bp = nullptr;
+    int2 *d_wrange = nullptr;
+    int *d_err = nullptr;
     int Zt_fwd = 0, Zt_b1 = 0;
 };
 
@@ -68,78 +79,205 @@ static void free_plan(gb_spect_plan *p) {
     if (!p) return;
     cudaFree(p->d_lin); cudaFree(p->d_theta_fwd); cudaFree(p->d_theta_bwd);
     cudaFree(p->d_taps_r); cudaFree(p->d_taps_z); cudaFree(p->d_A); cudaFree(p->d_group);
-    cudaFree(p->d_alist); cudaFree(p->d_partials); cudaFree(p->d_W); cudaFree(p->d_ratio);
+    cudaFree(p->d_alist); cudaFree(p->d_items); cudaFree(p->d_ioff);
+    cudaFree(p->d_partials); cudaFree(p->d_W); cudaFree(p->d_ratio);
     cudaFree(p->d_bp);
+    cudaFree(p->d_wrange);
+    cudaFree(p->d_err);
     delete p;
 }
 
-// Chunks of x planes per angle so that the grid fills the GPU: the PSF kernels run one
-// 512-thread CTA per SM, the plain ones many 256-thread blocks per SM.
-static int fwd_chunks(const gb_spect_plan *p, int n_sel) {
-    int zs = p->dev.psf ? (p->nz + p->Zt_fwd - 1) / p->Zt_fwd : 1;
-    int c;
-    if (p->dev.psf) {
-        c = std::max(1, p->sm_count / std::max(1, n_sel * zs));
-    } else {
-        int gz = (p->N * p->nz + 255) / 256;
-        c = (8 * p->sm_count + n_sel * gz - 1) / std::max(1, n_sel * gz);
+// Rows of plane xp whose rotated sample can reach the object square (host, double
+// precision; only used to estimate work, the kernels decide exactly).
+static bool host_plane_rows(const gb_spect_plan *p, int a, int xp, int ylo, int yhi,
+                            double margin, int &ra, int &rb) {
+    const float *th = p->h_theta_fwd.data() + 6 * a;
+    const double half = (p->Lp - 1) / 2.0;
+    auto coords = [&](int y, double &ix, double &iy) {
+        double gx = (double)th[0] * p->h_lin[y] + (double)th[1] * p->h_lin[xp] + th[2];
+        double gy = (double)th[3] * p->h_lin[y] + (double)th[4] * p->h_lin[xp] + th[5];
+        ix = (gx + 1) * half;
+        iy = (gy + 1) * half;
+    };
+    const int y0 = ylo, y1 = yhi - 1;
+    double pa[2], pb[2];
+    coords(y0, pa[0], pa[1]);
+    coords(y1, pb[0], pb[1]);
+    const double lo = p->pad - 1 - margin, hi = p->pad + p->N + margin;
+    double t0 = 0, t1 = 1;
+    for (int k = 0; k < 2; k++) {
+        double d = pb[k] - pa[k];
+        if (std::fabs(d) < 1e-12) {
+            if (pa[k] < lo || pa[k] > hi) return false;
+        } else {
+            double ta = (lo - pa[k]) / d, tb = (hi - pa[k]) / d;
+            if (ta > tb) std::swap(ta, tb);
+            t0 = std::max(t0, ta);
+            t1 = std::min(t1, tb);
+        }
     }
+    if (t0 > t1) return false;
+    ra = std::max(ylo, (int)std::floor(y0 + t0 * (y1 - y0)) - 1);
+    rb = std::min(yhi - 1, (int)std::ceil(y0 + t1 * (y1 - y0)) + 1);
+    return ra <= rb;
+}
+
+// Estimated work of every plane of angle a: forward (rows sampled + 2 x rows blurred)
+// or B1 (2 x rows blurred).
+static std::vector<double> plane_work(const gb_spect_plan *p, int a, bool fwd) {
+    std::vector<double> w(p->Lp, 1.0);
+    const int H = p->H;
+    const int ylo = std::max(0, p->pad - H), yhi = std::min(p->Lp, p->pad + p->N + H);
+    for (int xp = 0; xp < p->Lp; xp++) {
+        int ra, rb;
+        if (!host_plane_rows(p, a, xp, ylo, yhi, fwd ? 0.5 : 1.5, ra, rb)) continue;
+        if (fwd) {
+            int o = std::min(p->N, rb + H - p->pad + 1) - std::max(0, ra - H - p->pad);
+            w[xp] = 4.0 + (rb - ra + 1) + 2.0 * std::max(0, o);
+        } else {
+            w[xp] = 4.0 + 2.0 * (rb - ra + 1);
+        }
+    }
+    return w;
+}
+
+// Split [0, Lp) into c contiguous plane ranges of about equal work.
+static void split_planes(const std::vector<double> &w, int c, int slot,
+                         std::vector<int4> &out) {
+    const int L = (int)w.size();
+    double total = 0;
+    for (double v : w) total += v;
+    int x = 0;
+    double acc = 0;
+    int prev = 0;
+    for (int k = 1; k <= c; k++) {
+        int end = L;
+        if (k < c) {
+            const double target = total * k / c;
+            while (x < L && acc + w[x] <= target) acc += w[x++];
+            end = x;
+        }
+        out.push_back(make_int4(slot, prev, end, 0));
+        prev = end;
+    }
+}
+
+// Chunks per angle for the plain (no PSF) forward: many 256-thread blocks per SM.
+static int nopsf_chunks(const gb_spect_plan *p, int n_sel) {
+    int gz = (p->N * p->nz + 255) / 256;
+    int c = (8 * p->sm_count + n_sel * gz - 1) / std::max(1, n_sel * gz);
     return std::max(1, std::min(c, std::max(1, p->Lp / 4)));
 }
 
-static int b1_chunks(const gb_spect_plan *p, int n_sel) {
-    int zs = (p->nz + p->Zt_b1 - 1) / p->Zt_b1;
-    int c = std::max(1, p->sm_count / std::max(1, n_sel * zs));
-    return std::max(1, std::min(c, std::max(1, p->Lp / 4)));
-}
-
-static gb_status ensure_partials(gb_spect_plan *p, int n_sel) {
-    size_t need = (size_t)n_sel * fwd_chunks(p, n_sel) * p->N * p->nz;
-    if (need <= p->partials_cap) return GB_OK;
-    cudaFree(p->d_partials);
-    p->d_partials = nullptr;
-    GB_CUDA(cudaMalloc(&p->d_partials, need * sizeof(float)));
-    p->partials_cap = need;
-    return GB_OK;
+// Per-angle chunk counts so that n angles x chunks x z-slabs is about one wave.
+static std::vector<int> chunk_counts(const gb_spect_plan *p, int n, int zslabs) {
+    int T = std::max(n, p->sm_count / std::max(1, zslabs));
+    std::vector<int> c(n, T / n);
+    for (int i = 0; i < T % n; i++) c[i]++;
+    for (int &v : c) v = std::max(1, std::min(v, std::max(1, p->Lp / 4)));
+    return c;
 }
 
 static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
     std::vector<int> all;
-    p->list_off.clear();
-    p->list_len.clear();
-    p->list_off.push_back(0);
-    p->list_len.push_back(p->n_angles);
-    for (int a = 0; a < p->n_angles; a++) all.push_back(a);
+    std::vector<int4> items;
+    std::vector<int> ioff;
+    p->lists.clear();
+    std::vector<std::vector<int>> angle_lists;
+    {
+        std::vector<int> l;
+        for (int a = 0; a < p->n_angles; a++) l.push_back(a);
+        angle_lists.push_back(l);
+    }
     for (int s = 0; s < n_subsets; s++) {
-        p->list_off.push_back((int)all.size());
-        int len = 0;
-        for (int a = s; a < p->n_angles; a += n_subsets) {
-            all.push_back(a);
-            len++;
+        std::vector<int> l;
+        for (int a = s; a < p->n_angles; a += n_subsets) l.push_back(a);
+        angle_lists.push_back(l);
+    }
+    const bool psf = p->dev.psf;
+    const int zs_f = psf ? (p->nz + p->Zt_fwd - 1) / p->Zt_fwd : 1;
+    const int zs_b = psf ? (p->nz + p->Zt_b1 - 1) / p->Zt_b1 : 1;
+    std::vector<std::vector<double>> wf(p->n_angles), wb(p->n_angles);
+    if (psf)
+        for (int a = 0; a < p->n_angles; a++) {
+            wf[a] = plane_work(p, a, true);
+            wb[a] = plane_work(p, a, false);
         }
-        p->list_len.push_back(len);
+    size_t max_items = 0;
+    for (const auto &l : angle_lists) {
+        gb_spect_plan::List L;
+        L.alist_off = (int)all.size();
+        L.n = (int)l.size();
+        all.insert(all.end(), l.begin(), l.end());
+        // forward items
+        L.fitem_off = (int)items.size();
+        L.ioff_off = (int)ioff.size();
+        if (psf) {
+            std::vector<int> cnt = chunk_counts(p, L.n, zs_f);
+            for (int i = 0; i < L.n; i++) {
+                ioff.push_back((int)items.size() - L.fitem_off);
+                split_planes(wf[l[i]], cnt[i], i, items);
+            }
+        } else {
+            int c = nopsf_chunks(p, L.n);
+            for (int i = 0; i < L.n; i++) {
+                ioff.push_back((int)items.size() - L.fitem_off);
+                for (int k = 0; k < c; k++)
+                    items.push_back(make_int4(i, k * p->Lp / c, (k + 1) * p->Lp / c, 0));
+            }
+        }
+        L.n_fitems = (int)items.size() - L.fitem_off;
+        ioff.push_back(L.n_fitems);
+        max_items = std::max(max_items, (size_t)L.n_fitems);
+        // B1 items per angle group
+        for (int a0 = 0; a0 < L.n; a0 += p->G) {
+            int na = std::min(p->G, L.n - a0);
+            L.gitem_off.push_back((int)items.size());
+            if (psf) {
+                std::vector<int> cnt = chunk_counts(p, na, zs_b);
+                for (int i = 0; i < na; i++) split_planes(wb[l[a0 + i]], cnt[i], i, items);
+            }
+            L.n_gitems.push_back((int)items.size() - L.gitem_off.back());
+        }
+        p->lists.push_back(L);
     }
     cudaFree(p->d_alist);
+    cudaFree(p->d_items);
+    cudaFree(p->d_ioff);
     p->d_alist = nullptr;
+    p->d_items = nullptr;
+    p->d_ioff = nullptr;
     GB_CUDA(cudaMalloc(&p->d_alist, all.size() * sizeof(int)));
     GB_CUDA(cudaMemcpy(p->d_alist, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMalloc(&p->d_items, std::max<size_t>(1, items.size()) * sizeof(int4)));
+    if (!items.empty())
+        GB_CUDA(cudaMemcpy(p->d_items, items.data(), items.size() * sizeof(int4),
+                           cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMalloc(&p->d_ioff, ioff.size() * sizeof(int)));
+    GB_CUDA(cudaMemcpy(p->d_ioff, ioff.data(), ioff.size() * sizeof(int), cudaMemcpyHostToDevice));
     p->n_subsets = n_subsets;
-    for (size_t i = 0; i < p->list_len.size(); i++) {
-        gb_status st = ensure_partials(p, p->list_len[i]);
-        if (st != GB_OK) return st;
+    size_t need = max_items * p->N * p->nz;
+    if (need > p->partials_cap) {
+        cudaFree(p->d_partials);
+        p->d_partials = nullptr;
+        GB_CUDA(cudaMalloc(&p->d_partials, need * sizeof(float)));
+        p->partials_cap = need;
     }
     return GB_OK;
 }
 
+// List index of a subset (-1 = every angle), or -1 when out of range.
+static int list_index(const gb_spect_plan *p, int subset) {
+    if (subset < 0) return 0;
+    if (subset >= p->n_subsets) return -1;
+    return subset + 1;
+}
+
 static bool select_list(const gb_spect_plan *p, int subset, const int **alist, int *n) {
-    if (subset < 0) {
-        *alist = p->d_alist;
-        *n = p->n_angles;
-        return true;
-    }
-    if (subset >= p->n_subsets) return false;
-    *alist = p->d_alist + p->list_off[subset + 1];
-    *n = p->list_len[subset + 1];
+    int li = list_index(p, subset);
+    if (li < 0) return false;
+    *alist = p->d_alist + p->lists[li].alist_off;
+    *n = p->lists[li].n;
     return true;
 }
 
@@ -244,6 +382,8 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     } while (0)
 
     const int n = d->n_angles, Lp = p->Lp;
+    p->h_theta_fwd.assign(d->theta_fwd, d->theta_fwd + 6 * n);
+    p->h_lin.assign(d->lin, d->lin + Lp);
     FAIL_CUDA(cudaMalloc(&p->d_lin, Lp * sizeof(float)));
     FAIL_CUDA(cudaMemcpy(p->d_lin, d->lin, Lp * sizeof(float), cudaMemcpyHostToDevice));
     FAIL_CUDA(cudaMalloc(&p->d_theta_fwd, 6 * n * sizeof(float)));
@@ -310,6 +450,12 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     FAIL_CUDA(cudaMalloc(&p->d_W, (size_t)p->G * Lp * g.nya * p->nz * sizeof(float)));
     FAIL_CUDA(cudaMalloc(&p->d_ratio, (size_t)n * p->N * p->nz * sizeof(float)));
     FAIL_CUDA(cudaMalloc(&p->d_bp, (size_t)p->N * p->N * p->nz * sizeof(float)));
+    FAIL_CUDA(cudaMalloc(&p->d_wrange, (size_t)p->G * Lp * sizeof(int2)));
+    FAIL_CUDA(cudaMemset(p->d_wrange, 0, (size_t)p->G * Lp * sizeof(int2)));
+    FAIL_CUDA(cudaMalloc(&p->d_err, sizeof(int)));
+    FAIL_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+    g.wrange = p->d_wrange;
+    g.err = p->d_err;
 #undef FAIL_CUDA
     gb_status st = upload_lists(p, 1);
     if (st != GB_OK) {
@@ -326,6 +472,13 @@ gb_status gb_spect_plan_destroy(gb_spect_plan *p) {
         cudaDeviceSynchronize();
         free_plan(p);
     }
+    return GB_OK;
+}
+
+gb_status gb_spect_device_status(gb_spect_plan *p, int32_t *code) {
+    clear_error();
+    GB_CHECK_ARG(p && code, "null argument");
+    GB_CUDA(cudaMemcpy(code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     return GB_OK;
 }
 
@@ -347,21 +500,18 @@ int32_t gb_spect_subset_size(const gb_spect_plan *p, int32_t subset) {
 
 static gb_status run_forward(gb_spect_plan *p, const float *obj, int subset, float *out,
                              int ratio, const float *gproj, const float *sadd, float *pred,
-                             cudaStream_t st, const int **alist_out, int *n_out) {
-    const int *alist;
-    int n;
-    if (!select_list(p, subset, &alist, &n)) {
+                             cudaStream_t st) {
+    const int li = list_index(p, subset);
+    if (li < 0) {
         set_error("subset %d out of range (n_subsets=%d)", subset, p->n_subsets);
         return GB_ERR_STATE;
     }
-    int ch = fwd_chunks(p, n);
-    gb_status s = ensure_partials(p, n);
-    if (s != GB_OK) return s;
-    GB_CUDA(launch_fwd(p->dev, obj, alist, n, ch, p->Zt_fwd, p->d_partials, st));
-    GB_CUDA(launch_reduce(n, ch, p->N * p->nz, p->d_partials, out, ratio, gproj, sadd, alist,
-                          pred, st));
-    if (alist_out) *alist_out = alist;
-    if (n_out) *n_out = n;
+    const gb_spect_plan::List &L = p->lists[li];
+    const int *alist = p->d_alist + L.alist_off;
+    GB_CUDA(launch_fwd(p->dev, obj, alist, p->d_items + L.fitem_off, L.n_fitems, p->Zt_fwd,
+                       p->d_partials, st));
+    GB_CUDA(launch_reduce(L.n, p->d_ioff + L.ioff_off, p->N * p->nz, p->d_partials, out, ratio,
+                          gproj, sadd, alist, pred, st));
     return GB_OK;
 }
 
@@ -369,21 +519,22 @@ gb_status gb_spect_forward(gb_spect_plan *p, const float *obj, float *proj, int3
                            gb_stream_t stream) {
     clear_error();
     GB_CHECK_ARG(p && obj && proj, "null argument");
-    return run_forward(p, obj, subset, proj, 0, nullptr, nullptr, nullptr, as_stream(stream),
-                       nullptr, nullptr);
+    return run_forward(p, obj, subset, proj, 0, nullptr, nullptr, nullptr, as_stream(stream));
 }
 
-// Back-project `proj` (rows = the angles of alist) in groups of G angles.
-static gb_status run_backward(gb_spect_plan *p, const float *proj, const int *alist, int n,
-                              int adjoint, float *out, int final_mode, UpdateArgs u,
-                              cudaStream_t st) {
+// Back-project `proj` (rows = the angles of list li) in groups of G angles.
+static gb_status run_backward(gb_spect_plan *p, const float *proj, int li, int adjoint,
+                              float *out, int final_mode, UpdateArgs u, cudaStream_t st) {
+    const gb_spect_plan::List &L = p->lists[li];
+    const int *alist = p->d_alist + L.alist_off;
+    const int n = L.n;
     const size_t NZ = (size_t)p->N * p->nz;
     const int n_groups = (n + p->G - 1) / p->G;
     if (adjoint) GB_CUDA(cudaMemsetAsync(out, 0, (size_t)p->N * NZ * sizeof(float), st));
     for (int gi = 0; gi < n_groups; gi++) {
         int a0 = gi * p->G, na = std::min(p->G, n - a0);
-        GB_CUDA(launch_b1(p->dev, proj + a0 * NZ, alist + a0, na, b1_chunks(p, na), p->Zt_b1,
-                          p->d_W, st));
+        GB_CUDA(launch_b1(p->dev, proj + a0 * NZ, alist + a0, na, p->d_items + L.gitem_off[gi],
+                          L.n_gitems[gi], p->Zt_b1, p->d_W, st));
         if (adjoint) {
             GB_CUDA(launch_b2_scatter(p->dev, p->d_W, alist + a0, na, out, st));
             continue;
@@ -407,14 +558,13 @@ gb_status gb_spect_backward(gb_spect_plan *p, const float *proj, float *obj, int
                             int32_t adjoint, gb_stream_t stream) {
     clear_error();
     GB_CHECK_ARG(p && proj && obj, "null argument");
-    const int *alist;
-    int n;
-    if (!select_list(p, subset, &alist, &n)) {
+    const int li = list_index(p, subset);
+    if (li < 0) {
         set_error("subset %d out of range (n_subsets=%d)", subset, p->n_subsets);
         return GB_ERR_STATE;
     }
     UpdateArgs u{};
-    return run_backward(p, proj, alist, n, adjoint ? 1 : 0, obj, B2_WRITE, u, as_stream(stream));
+    return run_backward(p, proj, li, adjoint ? 1 : 0, obj, B2_WRITE, u, as_stream(stream));
 }
 
 gb_status gb_spect_osem_step(gb_spect_plan *p, float *obj, const float *g, const float *s,
@@ -423,14 +573,12 @@ gb_status gb_spect_osem_step(gb_spect_plan *p, float *obj, const float *g, const
     clear_error();
     GB_CHECK_ARG(p && obj && g && nbp, "null argument");
     cudaStream_t st = as_stream(stream);
-    const int *alist;
-    int n;
-    gb_status r = run_forward(p, obj, subset, p->d_ratio, 1, g, s, pred, st, &alist, &n);
+    gb_status r = run_forward(p, obj, subset, p->d_ratio, 1, g, s, pred, st);
     if (r != GB_OK) return r;
     UpdateArgs u{};
     u.f = obj;
     u.nbp = nbp;
-    return run_backward(p, p->d_ratio, alist, n, 0, obj, B2_OSEM, u, st);
+    return run_backward(p, p->d_ratio, list_index(p, subset), 0, obj, B2_OSEM, u, st);
 }
 
 static void rdp_weights(float dx, float dy, float dz, float w[26]) {
@@ -453,9 +601,7 @@ gb_status gb_spect_bsrem_step(gb_spect_plan *p, const float *in, float *out, con
     GB_CHECK_ARG(p && in && out && g && nbp && nbp_sum, "null argument");
     GB_CHECK_ARG(in != out, "BSREM needs distinct input and output objects");
     cudaStream_t st = as_stream(stream);
-    const int *alist;
-    int n;
-    gb_status r = run_forward(p, in, subset, p->d_ratio, 1, g, s, nullptr, st, &alist, &n);
+    gb_status r = run_forward(p, in, subset, p->d_ratio, 1, g, s, nullptr, st);
     if (r != GB_OK) return r;
     UpdateArgs u{};
     u.f_in = in;
@@ -473,7 +619,7 @@ gb_status gb_spect_bsrem_step(gb_spect_plan *p, const float *in, float *out, con
         u.fov = prior->fov_scale;
         rdp_weights(p->dx, p->dy, p->dz, u.w26);
     }
-    return run_backward(p, p->d_ratio, alist, n, 0, out, B2_BSREM, u, st);
+    return run_backward(p, p->d_ratio, list_index(p, subset), 0, out, B2_BSREM, u, st);
 }
 
 gb_status gb_rdp_gradient(const float *f, float *grad, int32_t nx, int32_t ny, int32_t nz,
@@ -494,3 +640,21 @@ gb_status gb_rdp_gradient(const float *f, float *grad, int32_t nx, int32_t ny, i
 }
 
 }  // extern "C"
+
+namespace gb {
+
+bool plan_forward_args(const gb_spect_plan *p, int subset, FwdArgs *a) {
+    const int li = p ? list_index(p, subset) : -1;
+    if (li < 0) return false;
+    const gb_spect_plan::List &L = p->lists[li];
+    a->g = p->dev;
+    a->alist = p->d_alist + L.alist_off;
+    a->n_sel = L.n;
+    a->items = p->d_items + L.fitem_off;
+    a->n_items = L.n_fitems;
+    a->ioff = p->d_ioff + L.ioff_off;
+    a->Zt = p->Zt_fwd;
+    return true;
+}
+
+}  // namespace gb

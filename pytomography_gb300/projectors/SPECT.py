@@ -142,6 +142,12 @@ class SPECTSystemMatrix(SystemMatrix):
                 pass
             self._plan = None
 
+    def device_status(self) -> int:
+        """Device error word of the plan (0 = no kernel gave up on a bounded wait)."""
+        code = ctypes.c_int32(0)
+        _lib.check(self._lib.gb_spect_device_status(self._plan, ctypes.byref(code)))
+        return int(code.value)
+
     # ------------------------------------------------------------ subsets
     def set_n_subsets(self, n_subsets: int) -> None:
         indices = torch.arange(self.proj_meta.shape[0]).to(torch.long).to(self.device)

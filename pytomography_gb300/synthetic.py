@@ -98,3 +98,18 @@ def poisson_projections(H, w: SpectWorkload) -> torch.Tensor:
     clean = H.forward(f).cpu()
     gen = torch.Generator().manual_seed(w.poisson_seed)
     return torch.poisson(clean, generator=gen)
+
+
+def config5(seed: int = 5, n_recons: int = 32, sizes=(64, 96, 128), angle_counts=(60, 90, 120)):
+    """Uneven serving mix: n_recons seeded reconstructions with object sizes drawn from
+    ``sizes`` and angle counts from ``angle_counts``, 4.42 mm voxels, 22 cm radius,
+    attenuation + PSF as in the 128^3 workload (bodies scaled to the object), 10 subsets."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_recons):
+        n = int(rng.choice(sizes))
+        a = int(rng.choice(angle_counts))
+        w = config2(seed=seed * 1000 + i, n=n, n_angles=a)
+        w.poisson_seed = seed * 1000 + i
+        out.append(w)
+    return out

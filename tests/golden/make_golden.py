@@ -204,8 +204,47 @@ def theta_case(out):
     print("wrote theta")
 
 
+def autograd_case(out):
+    """Gradient of the Poisson NLL through the reference forward projector, by torch
+    autograd through its undecorated transforms (the reference wraps them in no_grad)."""
+    from pytomography.transforms.shared import RotationTransform
+    set_precision(torch.float64)
+    shape, dr = (16, 16, 10), (0.48, 0.48, 0.48)
+    angles = [float(a) for a in np.linspace(0, 360, 9)[:-1]]
+    f_np, mu_np = ellipsoid_phantom(shape, dr, 31)
+    f_np = f_np + 0.2
+    om = SPECTObjectMeta(list(dr), shape)
+    pm = SPECTProjMeta(shape[1:], list(dr[:2]), angles, radii=[20.0] * len(angles))
+    att = SPECTAttenuationTransform(torch.tensor(mu_np))
+    psf = SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)))
+    H = SPECTSystemMatrix([att, psf], [], om, pm)
+    rng = np.random.default_rng(32)
+    g_np = rng.poisson(H.forward(torch.tensor(f_np)).numpy() * 3).astype(np.float64)
+    saved = {}
+    for cls, name in ((RotationTransform, "backward"), (type(att), "forward"),
+                      (type(psf), "forward")):
+        saved[(cls, name)] = getattr(cls, name)
+        setattr(cls, name, getattr(cls, name).__wrapped__)
+    try:
+        f = torch.tensor(f_np, requires_grad=True)
+        pred = H.forward(f)
+        g = torch.tensor(g_np)
+        nll = (pred - g * torch.log(pred + 1e-11)).sum()
+        nll.backward()
+        grad = f.grad.numpy()
+    finally:
+        for (cls, name), fn in saved.items():
+            setattr(cls, name, fn)
+    set_precision(torch.float32)
+    np.savez_compressed(os.path.join(out, "autograd.npz"), shape=np.array(shape),
+                        dr=np.array(dr), angles=np.array(angles), radii=np.full(len(angles), 20.0),
+                        object=f_np, mu=mu_np, projections=g_np, nll=float(nll), grad=grad)
+    print("wrote autograd")
+
+
 def main():
     out = HERE
+    autograd_case(out)
     theta_case(out)
     torch.manual_seed(0)
     spect_case("spect_even", (16, 16, 12), (0.48, 0.48, 0.48),

@@ -136,3 +136,4 @@ def test_full_size_geometries_vs_oracle(n, nz, n_angles, order, radius, dr, cuda
     assert rel_l2(bwd, o.backward(g, idx)) < TOL
     adj = H.backward_adjoint(torch.tensor(g, dtype=torch.float32, device=cuda), sub).cpu().numpy()
     assert rel_l2(adj, o.adjoint(g, idx)) < TOL
+    assert H.device_status() == 0
