@@ -143,13 +143,16 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
                 for (int i = 0; i < OB + K - 1; i++) win[i] = sp[i * SC];
                 float *tq = Tt + c * TS + ob * OB;
+float o[OB];
 #pragma unroll
-                for (int j = 0; j < OB; j++) {
-                    float o = 0.f;
+                for (int j = 0; j < OB; j++) o[j] = 0.f;
+                // tap-outer order: OB independent accumulation chains per tap
 #pragma unroll
-                    for (int t = 0; t < K; t++) o = fmaf(w[t], win[j + t], o);
-                    tq[j] = o;
-                }
+                for (int t = 0; t < K; t++)
+#pragma unroll
+                    for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
+#pragma unroll
+                for (int j = 0; j < OB; j++) tq[j] = o[j];
             }
         }
         __syncthreads();
@@ -190,12 +193,11 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
                     for (int i = 0; i < OB + K - 1; i++) win[i] = tq[i * TS];
 #pragma unroll
-                    for (int j = 0; j < OB; j++) {
-                        float s2 = 0.f;
+                    for (int j = 0; j < OB; j++) o[j] = 0.f;
 #pragma unroll
-                        for (int t = 0; t < K; t++) s2 = fmaf(w[t], win[j + t], s2);
-                        o[j] = s2;
-                    }
+                    for (int t = 0; t < K; t++)
+#pragma unroll
+                        for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
                 } else {
 #pragma unroll
                     for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + H) * TS + o_row];

@@ -30,6 +30,7 @@ __device__ unsigned long long g_fwd_phase_cycles[4096 * 8];
 #else
 #define GB_T(k, v) \
     do {           \
+        (void)(v); \
     } while (0)
 #define GB_NOW() 0LL
 #endif
@@ -266,13 +267,16 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
                 for (int i = 0; i < OB + K - 1; i++) win[i] = sp[i * SC];
                 float *tq = Tt + c * TS + yb * OB;
+float o[OB];
 #pragma unroll
-                for (int j = 0; j < OB; j++) {
-                    float o = 0.f;
+                for (int j = 0; j < OB; j++) o[j] = 0.f;
+                // tap-outer order: OB independent accumulation chains per tap
 #pragma unroll
-                    for (int t = 0; t < K; t++) o = fmaf(w[t], win[j + t], o);
-                    tq[j] = o;
-                }
+                for (int t = 0; t < K; t++)
+#pragma unroll
+                    for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
+#pragma unroll
+                for (int j = 0; j < OB; j++) tq[j] = o[j];
             }
         }
         __syncthreads();
@@ -304,12 +308,11 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
                         for (int i = 0; i < OB + K - 1; i++) win[i] = tq[i * TS];
 #pragma unroll
-                        for (int j = 0; j < OB; j++) {
-                            float s2 = 0.f;
+                        for (int j = 0; j < OB; j++) o[j] = 0.f;
 #pragma unroll
-                            for (int t = 0; t < K; t++) s2 = fmaf(w[t], win[j + t], s2);
-                            o[j] = s2;
-                        }
+                        for (int t = 0; t < K; t++)
+#pragma unroll
+                            for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
                     } else {
 #pragma unroll
                         for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + HP) * TS + y];

@@ -121,11 +121,10 @@ __device__ __forceinline__ float sample(const float *__restrict__ src, int rows,
 __device__ __forceinline__ bool sample4(const float *__restrict__ src, int rows, int cols, int nz,
                                         int row_off, int col_off, const Bilin &b, int z,
                                         float4 &out) {
+    // branch-free: the four (predicated) loads of a sample can be in flight together
     int r = b.r0 - row_off, c = b.c0 - col_off;
     bool r0 = (unsigned)r < (unsigned)rows, r1 = (unsigned)(r + 1) < (unsigned)rows;
     bool c0 = (unsigned)c < (unsigned)cols, c1 = (unsigned)(c + 1) < (unsigned)cols;
-    out = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!((r0 || r1) && (c0 || c1))) return false;
     const float *p = src + ((long long)r * cols + c) * nz + z;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 vnw = (r0 && c0) ? __ldg(reinterpret_cast<const float4 *>(p)) : zero;
@@ -137,7 +136,7 @@ __device__ __forceinline__ bool sample4(const float *__restrict__ src, int rows,
     out.y = bilin_combine(b, vnw.y, vne.y, vsw.y, vse.y);
     out.z = bilin_combine(b, vnw.z, vne.z, vsw.z, vse.z);
     out.w = bilin_combine(b, vnw.w, vne.w, vsw.w, vse.w);
-    return true;
+    return (r0 || r1) && (c0 || c1);
 }
 
 // Same as sample4 for the back-projection stack W of one angle slot: plane r holds data
