@@ -93,6 +93,16 @@ int32_t gb_spect_subset_size(const gb_spect_plan *plan, int32_t subset);
 gb_status gb_spect_forward(gb_spect_plan *plan, const float *object, float *proj,
                            int32_t subset, gb_stream_t stream);
 
+/* Same projection as gb_spect_forward, for callers that must not allocate device memory
+ * while they run (graph-captured or pool-restricted code, processes whose memory belongs
+ * to another allocator).  No counterpart in the reference.  Its partial sums use a fixed
+ * 16 MiB device array compiled into the library instead of the plan's scratch; calls
+ * needing more than 4,194,304 floats of partials (the plan's work items for the subset,
+ * at least one per angle, times nx * nz) return GB_ERR_SHAPE.  Calls share that array: overlapping calls on the GPU race.  The first
+ * call on a device looks the array up (cudaGetSymbolAddress); make it before any stream
+ * capture. */
+gb_status gb_spect_forward_static(gb_spect_plan *plan, const float *object, float *proj,
+                                  int32_t subset, gb_stream_t stream);
 
 /* Back projection proj [n_sel][ny][nz] -> object [nx][ny][nz] (device, overwritten).
  * adjoint = 0: the reference back-projector, which rotates back with bilinear
