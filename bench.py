@@ -33,6 +33,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "OSEM subiter/s at 128^3x120 ang (att+PSF)"
+# DRAM bytes (read + write) of one 12-angle k_fwd_psf launch from the ncu capture summarised
+# in profiles/spect_osem_128cube_120ang.md
+FWD_DRAM_BYTES_PER_LAUNCH = 114.885e6 + 3.163e6
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -406,7 +409,8 @@ def main():
                     "what": "OSEM(4,10) from host tensors incl. plan build and normalisation"},
             "roofline": {"bound": "hbm", "kernel": "forward projector (k_fwd_psf + k_reduce)",
                          "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                         "peak_kind": peak_kind, "traffic": None,
+                         "peak_kind": peak_kind, "traffic": FWD_DRAM_BYTES_PER_LAUNCH,
+                         "traffic_source": "ncu dram__bytes_read+write, one launch",
                          "alg_bytes_per_launch": fwd_bytes, "launch_ms": fwd_ms},
             "backward_ms": bwd_ms,
             "alg_gbs_per_subiter": sub_bytes / (fused_ms / 1000) / 1e9,

@@ -13,12 +13,30 @@
 //   k_b2_gather           : object frame, bilinear gather of W at the back-rotation
 //                           (reference operator), fused OSEM / BSREM update epilogue
 //   k_b2_scatter          : exact transpose of the forward's gather (adjoint operator)
+#include "spect_blur.cuh"
 #include "spect_kernels.cuh"
 #include "spect_launch.h"
 
 namespace gb {
 
 static bool b1_fixed(int K, int N, int Zt);
+
+#ifdef GB_PHASE_TIMING
+// Per-CTA cycle counts of k_b1_psf (diagnostic builds only): [1] phase 1 (S load),
+// [2] y blur, [3] z blur + W store, [4] planes, [5] total.
+__device__ unsigned long long g_b1_phase_cycles[4096 * 8];
+#define GB_B1T(k, v)                            \
+    do {                                        \
+        if (threadIdx.x == 0) tacc[k] += (v);   \
+    } while (0)
+#define GB_B1NOW() clock64()
+#else
+#define GB_B1T(k, v) \
+    do {             \
+        (void)(v);   \
+    } while (0)
+#define GB_B1NOW() 0LL
+#endif
 
 // ------------------------------------------------------------- attenuation
 // A[a][xp][y][z] = exp(-(sum_{k>=xp} mu_rot[k]*dx - mu_rot[xp]*dx/2)) for the stored
@@ -102,7 +120,13 @@ __global__ void __launch_bounds__(512, 1)
     for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * ga + k];
     int2 *wr = g.wrange + (size_t)slot * g.Lp;
     int parity = 0;
+#ifdef GB_PHASE_TIMING
+    unsigned long long tacc[6] = {0, 0, 0, 0, 0, 0};
+    const long long t_start = clock64();
+#endif
+    long long t0 = GB_B1NOW();
     for (int xp = x0; xp < x1; ++xp) {
+        t0 = GB_B1NOW();
         // rows of this plane the gather can sample (object square + 1.5 px margin)
         int ra, rb;
         if (!plane_rows(g, th, xp, g.ya_lo, g.ya_hi, 1.5f, ra, rb)) {
@@ -129,99 +153,108 @@ __global__ void __launch_bounds__(512, 1)
         }
         __syncthreads();
         {
-            float w[K];
-#pragma unroll
-            for (int t = 0; t < K; t++) w[t] = tap[t];
-            const int nb = b_hi - b_lo;
-            const int ncc = (ncol + 31) >> 5;
-            for (int p = warp; p < ncc * nb; p += nwarp) {
-                const int cc = p % ncc, ob = b_lo + p / ncc;
-                const int c = cz_lo + (cc << 5) + lane;
-                if (c >= cz_hi) continue;
-                const float *sp = S + ob * OB * SC + c;
-                float win[OB + K - 1];
-#pragma unroll
-                for (int i = 0; i < OB + K - 1; i++) win[i] = sp[i * SC];
-                float *tq = Tt + c * TS + ob * OB;
-float o[OB];
-#pragma unroll
-                for (int j = 0; j < OB; j++) o[j] = 0.f;
-                // tap-outer order: OB independent accumulation chains per tap
-#pragma unroll
-                for (int t = 0; t < K; t++)
-#pragma unroll
-                    for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
-#pragma unroll
-                for (int j = 0; j < OB; j++) tq[j] = o[j];
-            }
+            long long t1 = GB_B1NOW();
+            GB_B1T(1, t1 - t0);
+            t0 = t1;
         }
+        constexpr int KK0 = 2 * tier_half(K, 0) + 1, KK1 = 2 * tier_half(K, 1) + 1;
+        int tier = 2;
+        if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : 2;
+        if (tier == 0)
+            blur_first<K, KK0, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        else if (tier == 1)
+            blur_first<K, KK1, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        else
+            blur_first<K, K, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
         __syncthreads();
         {
-            float w[K];
-#pragma unroll
-            for (int t = 0; t < K; t++) w[t] = tap[K + t];
+            long long t1 = GB_B1NOW();
+            GB_B1T(2, t1 - t0);
+            t0 = t1;
+        }
+        {
             float *Wp = W + ((size_t)slot * g.Lp + xp) * g.nya * nz;
             const bool amul = Ap && g.att_first;
             // warp-tasks (32-row chunk, z block); lanes take consecutive output rows
             const int nrc = ((b_hi - b_lo) * OB + 31) >> 5;
-            for (int p = warp; p < nrc * (Z8 / OB); p += nwarp) {
-                const int rc = p % nrc, zb = p / nrc;
-                const int o_row = b_lo * OB + (rc << 5) + lane;
-                if (o_row >= b_hi * OB) continue;
-                const int y = g.pad - H + o_row;
-                const bool store = y >= ra && y <= rb;
-                const int zl0 = zb * OB;
-                const bool full = VEC && (zl0 + OB <= Zc);
-                const size_t rowoff = (size_t)(y - g.ya_lo) * nz + z0 + zl0;
-                float av[OB];
-                if (store && amul) {  // issue the A loads before the blur arithmetic
-                    if (full) {
-#pragma unroll
-                        for (int j = 0; j < OB; j += 4) {
-                            float4 a4 = __ldg(reinterpret_cast<const float4 *>(Ap + rowoff + j));
-                            av[j] = a4.x; av[j + 1] = a4.y; av[j + 2] = a4.z; av[j + 3] = a4.w;
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < OB; j++) av[j] = zl0 + j < Zc ? Ap[rowoff + j] : 0.f;
-                    }
-                }
-                float o[OB];
-                if (g.psf2d) {
-                    const float *tq = Tt + zb * OB * TS + o_row;
-                    float win[OB + K - 1];
-#pragma unroll
-                    for (int i = 0; i < OB + K - 1; i++) win[i] = tq[i * TS];
-#pragma unroll
-                    for (int j = 0; j < OB; j++) o[j] = 0.f;
-#pragma unroll
-                    for (int t = 0; t < K; t++)
-#pragma unroll
-                        for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + H) * TS + o_row];
-                }
-                if (!store) continue;
-                if (amul) {
-#pragma unroll
-                    for (int j = 0; j < OB; j++) o[j] = __fmul_rn(o[j], av[j]);
-                }
-                if (full) {
-#pragma unroll
-                    for (int j = 0; j < OB; j += 4)
-                        *reinterpret_cast<float4 *>(Wp + rowoff + j) =
-                            make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < OB; j++)
-                        if (zl0 + j < Zc) Wp[rowoff + j] = o[j];
-                }
-            }
+#define GB_B1_PHASE3(KK)                                                                     \
+    {                                                                                        \
+        float w[KK];                                                                         \
+        load_taps<K, KK>(tap + K, w);                                                        \
+        for (int p = warp; p < nrc * (Z8 / OB); p += nwarp) {                                \
+            const int rc = p % nrc, zb = p / nrc;                                            \
+            const int o_row = b_lo * OB + (rc << 5) + lane;                                  \
+            if (o_row >= b_hi * OB) continue;                                                \
+            const int y = g.pad - H + o_row;                                                 \
+            const bool store = y >= ra && y <= rb;                                           \
+            const int zl0 = zb * OB;                                                         \
+            const bool full = VEC && (zl0 + OB <= Zc);                                       \
+            const size_t rowoff = (size_t)(y - g.ya_lo) * nz + z0 + zl0;                     \
+            float av[OB];                                                                    \
+            if (store && amul) { /* issue the A loads before the blur arithmetic */          \
+                if (full) {                                                                  \
+                    _Pragma("unroll") for (int j = 0; j < OB; j += 4) {                      \
+                        float4 a4 = __ldg(reinterpret_cast<const float4 *>(Ap + rowoff + j)); \
+                        av[j] = a4.x;                                                        \
+                        av[j + 1] = a4.y;                                                    \
+                        av[j + 2] = a4.z;                                                    \
+                        av[j + 3] = a4.w;                                                    \
+                    }                                                                        \
+                } else {                                                                     \
+                    _Pragma("unroll") for (int j = 0; j < OB; j++) av[j] =                   \
+                        zl0 + j < Zc ? Ap[rowoff + j] : 0.f;                                 \
+                }                                                                            \
+            }                                                                                \
+            float o[OB];                                                                     \
+            if (g.psf2d) {                                                                   \
+                blur_second<K, KK, OB>(Tt, w, TS, zb * OB, o_row, o);                        \
+            } else {                                                                         \
+                _Pragma("unroll") for (int j = 0; j < OB; j++) o[j] =                        \
+                    Tt[(zb * OB + j + H) * TS + o_row];                                      \
+            }                                                                                \
+            if (!store) continue;                                                            \
+            if (amul) {                                                                      \
+                _Pragma("unroll") for (int j = 0; j < OB; j++) o[j] = __fmul_rn(o[j], av[j]); \
+            }                                                                                \
+            if (full) {                                                                      \
+                _Pragma("unroll") for (int j = 0; j < OB; j += 4)                            \
+                    *reinterpret_cast<float4 *>(Wp + rowoff + j) =                           \
+                        make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);                     \
+            } else {                                                                         \
+                _Pragma("unroll") for (int j = 0; j < OB; j++) if (zl0 + j < Zc)             \
+                    Wp[rowoff + j] = o[j];                                                   \
+            }                                                                                \
+        }                                                                                    \
+    }
+            if (tier == 0)
+                GB_B1_PHASE3(KK0)
+            else if (tier == 1)
+                GB_B1_PHASE3(KK1)
+            else
+                GB_B1_PHASE3(K)
+#undef GB_B1_PHASE3
+        }
+        {
+            long long t1 = GB_B1NOW();
+            GB_B1T(3, t1 - t0);
+            GB_B1T(4, 1);
         }
         parity ^= 1;
     }
+#ifdef GB_PHASE_TIMING
+    if (threadIdx.x == 0 && blockIdx.x < 4096) {
+        tacc[5] = clock64() - t_start;
+        for (int k = 0; k < 6; k++)
+            g_b1_phase_cycles[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
+    }
+#endif
 }
+
+#ifdef GB_PHASE_TIMING
+extern "C" int gb_debug_b1_phase_cycles(unsigned long long *out, int n) {
+    return (int)cudaMemcpyFromSymbol(out, g_b1_phase_cycles, sizeof(unsigned long long) * (size_t)n);
+}
+#endif
 
 // -------------------------------------------------------------- B1 (no PSF)
 // W[slot][xp][y][z] = P[y - pad][z] * A (rows [pad, pad+N) are the stored rows).

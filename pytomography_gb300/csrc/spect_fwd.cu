@@ -12,6 +12,7 @@
 // blurs along y into a transposed buffer, blurs along z and accumulates the ray sum
 // in registers.  Partial sums of the chunks go to a scratch buffer and are reduced
 // in a fixed order by k_reduce (deterministic results).
+#include "spect_blur.cuh"
 #include "spect_kernels.cuh"
 #include "spect_launch.h"
 
@@ -118,16 +119,31 @@ __global__ void __launch_bounds__(512, 1)
     if (threadIdx.x == 0 && use_tma) mbar_init(bar, 1);
     float acc[NACC][OB];
     int ty[NACC], tz[NACC];  // phase-3 task (output row, z block) of this thread
+    // each warp owns whole z blocks and, for them, every 32-row chunk: restricting a
+    // plane's rows removes the same share of work from every warp
+    // (falls back to a linear task order when the rows need more chunks than tasks)
+    {
+        const int n_yc = (N8 + 31) >> 5;
+        const bool balanced = n_yc <= NACC;
 #pragma unroll
-    for (int k = 0; k < NACC; k++) {
-        const int task = threadIdx.x + k * blockDim.x;
-        ty[k] = task % N8;
-        tz[k] = task / N8;
+        for (int k = 0; k < NACC; k++) {
+            if (balanced) {
+                ty[k] = 32 * (k % n_yc) + lane;
+                tz[k] = warp + nwarp * (k / n_yc);
+                if (ty[k] >= N8 || k / n_yc >= NACC / n_yc) tz[k] = 1 << 20;  // no task
+            } else {
+                const int task = threadIdx.x + k * blockDim.x;
+                ty[k] = task % N8;
+                tz[k] = task / N8;
+            }
 #pragma unroll
-        for (int j = 0; j < OB; j++) acc[k][j] = 0.f;
+            for (int j = 0; j < OB; j++) acc[k][j] = 0.f;
+        }
     }
     __syncthreads();
 
+    bool failed = false;  // this thread's bounded wait gave up
+    unsigned failed_phase = 0;
     // next plane with any sample on the object, from xp on; rows in [ra, rb]
     auto next_plane = [&](int xp, int &ra, int &rb) {
         for (; xp < x1; ++xp)
@@ -136,7 +152,7 @@ __global__ void __launch_bounds__(512, 1)
     };
     // bulk-copy the attenuation rows [ra, rb] of plane xp into S (warp 0)
     auto issue_tma = [&](int xp, int ra, int rb) {
-        if (warp != 0) return;
+        if (warp != 0 || __any_sync(0xffffffffu, failed)) return;
         if (lane == 0) {
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(bar, row_bytes * (unsigned)(rb - ra + 1));
@@ -168,10 +184,12 @@ __global__ void __launch_bounds__(512, 1)
                 g.psf2d ? g.taps_z[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x] : 0.f;
         }
         if (use_tma) {
-            const bool ok = mbar_wait_bounded(bar, phase, 1u << 22);
-            if (__syncthreads_or(!ok)) {
-                if (threadIdx.x == 0 && g.err) atomicExch(g.err, GB_ERR_WAIT_TIMEOUT);
-                return;
+            // A thread whose bounded wait gives up flags the plan and stops waiting (its
+            // results are invalid); every thread still reaches every barrier.
+            if (!failed && !mbar_wait_bounded(bar, phase, 1u << 16)) {
+                failed = true;
+                failed_phase = phase;
+                if (g.err) atomicExch(g.err, GB_ERR_WAIT_TIMEOUT);
             }
             phase ^= 1u;
         }
@@ -190,13 +208,15 @@ __global__ void __launch_bounds__(512, 1)
                 for (int q = lane; q < nq; q += 32)
                     *reinterpret_cast<float4 *>(Sr + 4 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            for (int y0 = ra + warp; y0 <= rb; y0 += 4 * nwarp) {
+            // four consecutive rows per warp and batch: neighbouring rows share about half
+            // of their bilinear taps, which then hit in L1
+            for (int y0 = ra + 4 * warp; y0 <= rb; y0 += 4 * nwarp) {
                 int ys[4];
                 bool okr[4];
                 Bilin b[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
-                    ys[u] = y0 + u * nwarp;
+                    ys[u] = y0 + u;
                     okr[u] = ys[u] <= rb;
                     float ix, iy;
                     rot_coords(th, lr, g.lin[okr[u] ? ys[u] : y0], g.half, ix, iy);
@@ -250,35 +270,16 @@ __global__ void __launch_bounds__(512, 1)
         // output rows (local y in [0, N)) that the blurred plane can reach
         const int o_lo = max(0, ra - H - g.pad), o_hi = min(N, rb + H - g.pad + 1);
         const int b_lo = o_lo / OB, b_hi = (o_hi + OB - 1) / OB;
-        // phase 2: blur along y, write transposed.  Warp-tasks are (32-column chunk, row
-        // block); lanes take consecutive columns.
-        {
-            float w[K];
-#pragma unroll
-            for (int t = 0; t < K; t++) w[t] = tap[t];
-            const int nb = b_hi - b_lo;
-            const int ncc = (ncol + 31) >> 5;
-            for (int p = warp; p < ncc * nb; p += nwarp) {
-                const int cc = p % ncc, yb = b_lo + p / ncc;
-                const int c = cz_lo + (cc << 5) + lane;
-                if (c >= cz_hi) continue;
-                const float *sp = S + yb * OB * SC + c;
-                float win[OB + K - 1];
-#pragma unroll
-                for (int i = 0; i < OB + K - 1; i++) win[i] = sp[i * SC];
-                float *tq = Tt + c * TS + yb * OB;
-float o[OB];
-#pragma unroll
-                for (int j = 0; j < OB; j++) o[j] = 0.f;
-                // tap-outer order: OB independent accumulation chains per tap
-#pragma unroll
-                for (int t = 0; t < K; t++)
-#pragma unroll
-                    for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
-#pragma unroll
-                for (int j = 0; j < OB; j++) tq[j] = o[j];
-            }
-        }
+        // phase 2: blur along y, write transposed (tap tier of the plane)
+        constexpr int KK0 = 2 * tier_half(K, 0) + 1, KK1 = 2 * tier_half(K, 1) + 1;
+        int tier = 2;
+        if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : 2;
+        if (tier == 0)
+            blur_first<K, KK0, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        else if (tier == 1)
+            blur_first<K, KK1, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        else
+            blur_first<K, K, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
         __syncthreads();
         {
             long long t1 = GB_NOW();
@@ -293,43 +294,39 @@ float o[OB];
         if (use_tma && nxp < x1) issue_tma(nxp, nra, nrb);
         // phase 3: blur along z (2D PSF), optional attenuation after the PSF, accumulate
         {
-            float w[K];
-#pragma unroll
-            for (int t = 0; t < K; t++) w[t] = tap[K + t];
             const int y_lo = b_lo * OB, y_hi = b_hi * OB;
-#pragma unroll
-            for (int k = 0; k < NACC; k++) {
-                const int y = ty[k], zb = tz[k];
-                if (zb * OB < Z8 && y >= y_lo && y < y_hi) {
-                    float o[OB];
-                    if (g.psf2d) {
-                        const float *tq = Tt + (zb * OB + HP - H) * TS + y;
-                        float win[OB + K - 1];
-#pragma unroll
-                        for (int i = 0; i < OB + K - 1; i++) win[i] = tq[i * TS];
-#pragma unroll
-                        for (int j = 0; j < OB; j++) o[j] = 0.f;
-#pragma unroll
-                        for (int t = 0; t < K; t++)
-#pragma unroll
-                            for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + HP) * TS + y];
-                    }
-                    if (Ap && !g.att_first && y < N) {
-#pragma unroll
-                        for (int j = 0; j < OB; j++) {
-                            int z = z0 + zb * OB + j;
-                            if (z < nz)
-                                o[j] = __fmul_rn(
-                                    o[j], Ap[(size_t)(g.pad + y - g.ya_lo) * nz + z]);
-                        }
-                    }
-#pragma unroll
-                    for (int j = 0; j < OB; j++) acc[k][j] += o[j];
-                }
-            }
+#define GB_FWD_PHASE3(KK)                                                                   \
+    {                                                                                       \
+        float w[KK];                                                                        \
+        load_taps<K, KK>(tap + K, w);                                                       \
+        _Pragma("unroll") for (int k = 0; k < NACC; k++) {                                  \
+            const int y = ty[k], zb = tz[k];                                                \
+            if (zb * OB < Z8 && y >= y_lo && y < y_hi) {                                    \
+                float o[OB];                                                                \
+                if (g.psf2d) {                                                              \
+                    blur_second<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, o);              \
+                } else {                                                                    \
+                    _Pragma("unroll") for (int j = 0; j < OB; j++) o[j] =                   \
+                        Tt[(zb * OB + j + HP) * TS + y];                                    \
+                }                                                                           \
+                if (Ap && !g.att_first && y < N) {                                          \
+                    _Pragma("unroll") for (int j = 0; j < OB; j++) {                        \
+                        int z = z0 + zb * OB + j;                                           \
+                        if (z < nz)                                                         \
+                            o[j] = __fmul_rn(o[j], Ap[(size_t)(g.pad + y - g.ya_lo) * nz + z]); \
+                    }                                                                       \
+                }                                                                           \
+                _Pragma("unroll") for (int j = 0; j < OB; j++) acc[k][j] += o[j];           \
+            }                                                                               \
+        }                                                                                   \
+    }
+            if (tier == 0)
+                GB_FWD_PHASE3(KK0)
+            else if (tier == 1)
+                GB_FWD_PHASE3(KK1)
+            else
+                GB_FWD_PHASE3(K)
+#undef GB_FWD_PHASE3
         }
         {
             long long t1 = GB_NOW();
@@ -341,6 +338,7 @@ float o[OB];
         ra = nra;
         rb = nrb;
     }
+    if (failed) mbar_wait_bounded(bar, failed_phase, 1u << 16);
 #ifdef GB_PHASE_TIMING
     if (threadIdx.x == 0 && blockIdx.x < 4096) {
         tacc[5] = clock64() - t_start;

@@ -35,6 +35,7 @@ struct SpectDev {
     const float *taps_r;    // [n_groups][Lp][K]
     const float *taps_z;    // [n_groups][Lp][K]
     const int *group;       // [n_angles]
+    const signed char *tier;  // [n_groups][Lp] tap tier of each plane, or null (full taps)
     int K;                  // taps per row (odd)
     int att;                // attenuation present
     int att_first;          // forward order: attenuation before PSF ("ap")
@@ -251,16 +252,18 @@ __device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned
         : "memory");
 }
 
-// Wait for phase `parity` of `bar`, giving up after `limit` polls.
+// Wait for phase `parity` of `bar`, giving up after `limit` polls; each poll may suspend
+// the thread for up to 20 us while the phase is incomplete (no busy spinning).
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity,
                                                   unsigned limit) {
     for (unsigned i = 0; i < limit; i++) {
         unsigned ok;
         asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(ok)
-            : "r"(smem_u32(bar)), "r"(parity)
+            : "r"(smem_u32(bar)), "r"(parity), "r"(20000u)
             : "memory");
         if (ok) return true;
     }

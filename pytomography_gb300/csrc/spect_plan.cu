@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "spect_blur.cuh"
 #include "spect_launch.h"
 
 namespace gb {
@@ -50,6 +51,7 @@ struct gb_spect_plan {
     // device tables
     float *d_lin = nullptr, *d_theta_fwd = nullptr, *d_theta_bwd = nullptr;
     float *d_taps_r = nullptr, *d_taps_z = nullptr, *d_A = nullptr;
+    signed char *d_tier = nullptr;
     int *d_group = nullptr;
     // angle lists: [all][subset 0][subset 1]..., with their work items
     int *d_alist = nullptr;
@@ -79,6 +81,7 @@ static void free_plan(gb_spect_plan *p) {
     if (!p) return;
     cudaFree(p->d_lin); cudaFree(p->d_theta_fwd); cudaFree(p->d_theta_bwd);
     cudaFree(p->d_taps_r); cudaFree(p->d_taps_z); cudaFree(p->d_A); cudaFree(p->d_group);
+    cudaFree(p->d_tier);
     cudaFree(p->d_alist); cudaFree(p->d_items); cudaFree(p->d_ioff);
     cudaFree(p->d_partials); cudaFree(p->d_W); cudaFree(p->d_ratio);
     cudaFree(p->d_bp);
@@ -291,9 +294,13 @@ static int choose_zt(int K, int N, int nz, bool fwd) {
         int z = std::min(zt, (nz + OB - 1) / OB * OB);
         size_t sm = fwd ? fwd_psf_smem_bytes(K, N, z) : b1_psf_smem_bytes(K, N, z);
         if (sm > cap) break;
-        if (fwd) {
-            int N8 = (N + OB - 1) / OB * OB;
-            if ((long)N8 * (z / OB) > 512L * (32 / OB)) break;
+        if (fwd) {  // phase-3 tasks of k_fwd_psf: 16 warps x (32 / OB) tasks per thread
+            const int N8 = (N + OB - 1) / OB * OB, NACC = 32 / OB, n_yc = (N8 + 31) / 32;
+            if (n_yc <= NACC) {
+                if (z / OB > 16 * (NACC / n_yc)) break;
+            } else if ((long)N8 * (z / OB) > 512L * NACC) {
+                break;
+            }
         }
         best = z;
         if (z >= nz) break;
@@ -414,6 +421,22 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
                     }
                 }
             }
+        // tap tier of every plane: the narrowest unrolled loop that holds its nonzero taps
+        std::vector<signed char> tier((size_t)ng * Lp, 2);
+        const int Hk = K / 2;
+        for (int gi = 0; gi < ng; gi++)
+            for (int x = 0; x < Lp; x++) {
+                int h = 0;
+                for (int which = 0; which < 2; which++) {
+                    const std::vector<float> &tab = which == 0 ? tr : tz;
+                    for (int t = 0; t < K; t++)
+                        if (tab[((size_t)gi * Lp + x) * K + t] != 0.f) h = std::max(h, std::abs(t - Hk));
+                }
+                tier[(size_t)gi * Lp + x] =
+                    h <= tier_half(K, 0) ? 0 : (h <= tier_half(K, 1) ? 1 : 2);
+            }
+        FAIL_CUDA(cudaMalloc(&p->d_tier, tier.size()));
+        FAIL_CUDA(cudaMemcpy(p->d_tier, tier.data(), tier.size(), cudaMemcpyHostToDevice));
         FAIL_CUDA(cudaMalloc(&p->d_taps_r, tr.size() * sizeof(float)));
         FAIL_CUDA(cudaMemcpy(p->d_taps_r, tr.data(), tr.size() * sizeof(float), cudaMemcpyHostToDevice));
         FAIL_CUDA(cudaMalloc(&p->d_taps_z, tz.size() * sizeof(float)));
@@ -438,6 +461,7 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     g.group = p->d_group;
     g.taps_r = p->d_taps_r;
     g.taps_z = p->d_taps_z;
+    g.tier = p->d_tier;
     if (att) {
         size_t na = (size_t)n * Lp * g.nya * p->nz;
         FAIL_CUDA(cudaMalloc(&p->d_A, na * sizeof(float)));

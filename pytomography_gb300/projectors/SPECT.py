@@ -28,12 +28,13 @@ class SPECTSystemMatrix(SystemMatrix):
         object_meta, proj_meta: SPECT metadata.
         object_initial_based_on_camera_path: zero voxels the camera path never sees.
         psf_trunc_rel: PSF taps below this fraction of a plane's largest tap are skipped
-            (0 keeps the reference's full kernel).
+            (default 1e-7: changes projections by well under 1e-6 relative; 0 keeps every
+            tap of the reference's kernel).
     """
 
     def __init__(self, obj2obj_transforms, proj2proj_transforms, object_meta, proj_meta,
                  object_initial_based_on_camera_path: bool = False,
-                 psf_trunc_rel: float = 0.0) -> None:
+                 psf_trunc_rel: float = 1e-7) -> None:
         if proj2proj_transforms:
             raise NotImplementedError("proj2proj transforms are not part of the fused path")
         super().__init__(object_meta, proj_meta, obj2obj_transforms, proj2proj_transforms)

@@ -79,7 +79,7 @@ def config2(seed: int = 0, n: int = 128, n_angles: int = 120) -> SpectWorkload:
                          10, 2)
 
 
-def build_system_matrix(w: SpectWorkload, psf_trunc_rel: float = 0.0):
+def build_system_matrix(w: SpectWorkload, psf_trunc_rel: float = 1e-7):
     from .metadata.SPECT import SPECTObjectMeta, SPECTProjMeta, SPECTPSFMeta
     from .projectors.SPECT import SPECTSystemMatrix
     from .transforms.SPECT import SPECTAttenuationTransform, SPECTPSFTransform

@@ -81,6 +81,17 @@ def test_reference_backward_reproduces_reference_adjoint_gap(cuda):
     assert abs((a - b) - ref_gap) / abs(ref_gap) < 1e-2
 
 
+def test_exact_taps_and_truncated_taps_agree(cuda):
+    """psf_trunc_rel=0 keeps every tap of the reference kernel; the default truncation
+    (1e-7 of a plane's largest tap) changes the projection far below the 1e-5 budget."""
+    d = golden("spect_even")
+    f = t32(d["object"], cuda)
+    exact = make_sm(d, "att+psf", cuda, psf_trunc_rel=0.0).forward(f).cpu().numpy()
+    trunc = make_sm(d, "att+psf", cuda).forward(f).cpu().numpy()
+    assert rel_l2(exact, d["fwd_att+psf_f32"]) < TOL
+    assert rel_l2(trunc, exact) < 1e-6
+
+
 def test_deterministic(cuda):
     d = golden("spect_even")
     H = make_sm(d, "att+psf", cuda)
