@@ -39,6 +39,17 @@ FWD_DRAM_BYTES_PER_LAUNCH = 114.885e6 + 3.163e6
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
+def max_over_ranks(value: float, dist=None, device=None) -> float:
+    """Whole-job time: the maximum of a per-rank value over all ranks (replicas)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64,
+                     device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     try:
         with open(PEAKS) as fh:
@@ -156,6 +167,129 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _events_timer(fn, n, warm=3):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(n):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / n
+
+
+def run_pet(args, dev):
+    """TOF listmode OSEM: 200x200x96 image at 2 mm, 600 x 96 crystals (radius 400 mm),
+    10M events (20% randoms), 13 TOF bins, 20 subsets of 500k events.  A step is one
+    sub-iteration (TOF forward of the subset's events with the ratio epilogue, TOF back
+    projection, update).  The sensitivity image is replaced by ones (one-time cost,
+    excluded); the per-event additive term is the uniform randoms rate."""
+    import torch
+    from pytomography_gb300 import synthetic
+    from pytomography_gb300.likelihoods import PoissonLogLikelihood
+    w = synthetic.config3()
+    H = synthetic.build_pet_system_matrix(w)
+    E = w.events.shape[0]
+    H.norm_BP = torch.ones(w.shape, device=dev)
+    s = torch.full((E,), w.randoms_per_bin, device=dev)
+    lik = PoissonLogLikelihood(H, additive_term=s)
+    lik._set_n_subsets(w.n_subsets)
+    f = H._get_object_initial().contiguous()
+    nbps = [lik._get_normBP(k).contiguous() for k in range(w.n_subsets)]
+    k_state = [0]
+
+    def fused():
+        k = k_state[0] % w.n_subsets
+        H.osem_step(f, lik.projections, s, nbps[k], k)
+        k_state[0] += 1
+
+    def plain():
+        k = k_state[0] % w.n_subsets
+        grad = lik.compute_gradient(f, k)
+        f.add_(f * (1 / (nbps[k] + 1e-11)) * grad)
+        f[f <= 0] = 0
+        k_state[0] += 1
+
+    fused_ms = _events_timer(fused, args.steps)
+    plain_ms = _events_timer(plain, max(10, args.steps // 5))
+    fwd_ms = _events_timer(lambda: H.forward(f, 0), 20)
+    p0 = H.forward(f, 0)
+    bwd_ms = _events_timer(lambda: H.backward(p0, 0), 20)
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        from pytomography_gb300.metadata.PET import PETTOFMeta
+        cores = len(os.sched_getaffinity(0))
+        os.environ["OMP_NUM_THREADS"] = str(cores)
+        tm = PETTOFMeta(*w.tof)
+        o = oracle.PetLMOracle(w.shape, w.voxel_mm, H.proj_meta.scanner_lut.numpy(),
+                               tof=(w.tof[0], float(tm.bin_width), float(tm.sigma),
+                                    float(tm.center_offset), float(tm.n_sigmas)),
+                               precision="f32")
+        ev = w.events[0::w.n_subsets][:50000]
+        img = f.cpu().numpy()
+        t0 = time.perf_counter()
+        pr = o.forward(img, ev)
+        o.backward(1.0 / (pr + 1e-11), ev)
+        t = time.perf_counter() - t0
+        cpu = {"value": len(ev) / t / (E / w.n_subsets), "unit": "subiter/s", "cores": cores,
+               "kind": "port", "sample": "50k events of a subset, TOF forward + back projection, "
+                                         "float32 C/OpenMP oracle, scaled to 500k events"}
+    line = {"metric": "PET TOF listmode OSEM subiter/s (500k events per subset)",
+            "value": 1000.0 / fused_ms, "unit": "subiter/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": 3, "ms_per_step": fused_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w.name, "events": E, "subsets": w.n_subsets,
+                       "tof_bins": w.tof[0], "image": list(w.shape)},
+            "events_per_s": (E / w.n_subsets) / (fused_ms / 1000.0),
+            "plain": {"value": 1000.0 / plain_ms, "ms_per_step": plain_ms},
+            "forward_ms": fwd_ms, "backward_ms": bwd_ms, "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
+def run_autograd(args, dev):
+    """Differentiable SPECT at the 128^3 / 120-angle geometry: gradients of the Poisson NLL
+    of 8 objects through the autograd Function (forward + exact adjoint over all angles),
+    and fused BSREM sub-iterations with the RDP prior (beta 0.3, gamma 2)."""
+    import torch
+    from pytomography_gb300 import synthetic
+    from pytomography_gb300.algorithms import BSREM
+    from pytomography_gb300.autograd import poisson_nll
+    from pytomography_gb300.likelihoods import PoissonLogLikelihood
+    from pytomography_gb300.priors import RelativeDifferencePrior
+    ws = [synthetic.config2(seed=10 + i) for i in range(8)]
+    H = synthetic.build_system_matrix(ws[0])
+    gs = torch.stack([synthetic.poisson_projections(H, w).to(dev) for w in ws])
+    fb = torch.ones((8, *ws[0].shape), device=dev, requires_grad=True)
+
+    def grad_step():
+        fb.grad = None
+        poisson_nll(fb, H, gs).backward()
+
+    grad_ms = _events_timer(grad_step, max(3, args.steps // 20))
+    lik = PoissonLogLikelihood(H, gs[0])
+    alg = BSREM(lik, prior=RelativeDifferencePrior(beta=0.3, gamma=2))
+    alg(1, 10)  # warm-up, plans and normalisation
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n_it = 2
+    alg(n_it, 10)
+    torch.cuda.synchronize()
+    bsrem_ms = (time.perf_counter() - t0) * 1000.0 / (n_it * 10)
+    line = {"metric": "Poisson-NLL object gradients/s (128^3, 120 angles, att+PSF)",
+            "value": 8 * 1000.0 / grad_ms, "unit": "gradients/s", "n_gpus": 1,
+            "steps": max(3, args.steps // 20), "warmup": 3, "ms_per_step": grad_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "8 objects x 128^3, 120 angles, att+PSF, autograd",
+                       "bsrem": "RDP beta 0.3 gamma 2, 10 subsets"},
+            "bsrem": {"value": 1000.0 / bsrem_ms, "unit": "subiter/s", "ms_per_step": bsrem_ms}}
+    print(json.dumps(line))
+
+
 def run_serving(args, dev):
     """32 uneven reconstructions (sizes 64/96/128^3, 60/90/120 angles, att + PSF, 10
     subsets): sub-iterations summed over reconstructions per second, batched (graphs over
@@ -228,9 +362,11 @@ def main():
     ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
     ap.add_argument("--profile-case", action="store_true",
                     help="run 3 fused sub-iterations of the workload and exit (for ncu)")
-    ap.add_argument("--workload", default="osem128", choices=["osem128", "serving"],
+    ap.add_argument("--workload", default="osem128",
+                    choices=["osem128", "serving", "pet", "autograd"],
                     help="osem128: the 128^3 x 120-angle reconstruction (default); serving: "
-                         "32 uneven reconstructions, batched vs plain")
+                         "32 uneven reconstructions, batched vs plain; pet: TOF listmode OSEM "
+                         "(10M events); autograd: Poisson-NLL gradients of 8 objects + BSREM")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -256,6 +392,10 @@ def main():
     _lib.load()
     if args.workload == "serving":
         return run_serving(args, dev)
+    if args.workload == "pet":
+        return run_pet(args, dev)
+    if args.workload == "autograd":
+        return run_autograd(args, dev)
 
     w = synthetic.config2()
     H = synthetic.build_system_matrix(w)
@@ -327,11 +467,7 @@ def main():
     torch.cuda.synchronize()
     if clocks:
         clocks.__exit__()
-    ms = s0.elapsed_time(s1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t)
+    ms = max_over_ranks(s0.elapsed_time(s1), dist, dev)
     fused_ms = ms / args.steps
     value = world * args.steps / (ms / 1000.0)
 

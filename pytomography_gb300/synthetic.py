@@ -113,3 +113,112 @@ def config5(seed: int = 5, n_recons: int = 32, sizes=(64, 96, 128), angle_counts
         w.poisson_seed = seed * 1000 + i
         out.append(w)
     return out
+
+
+# ------------------------------------------------------------------- PET listmode
+PET_INFO = dict(crystalTransNr=1, crystalTransSpacing=4.0, submoduleTransNr=1,
+                submoduleTransSpacing=0.0, moduleTransNr=1, moduleTransSpacing=0.0,
+                rsectorTransNr=600, crystalAxialNr=96, crystalAxialSpacing=4.0,
+                submoduleAxialNr=1, submoduleAxialSpacing=0.0, moduleAxialNr=1,
+                moduleAxialSpacing=0.0, rsectorAxialNr=1, radius=400.0, firstCrystalAxis=1,
+                NrCrystalsPerRing=600, NrRings=96)
+
+
+@dataclass
+class PetWorkload:
+    name: str
+    shape: tuple
+    voxel_mm: tuple
+    info: dict
+    events: np.ndarray      # [E, 3] int64: crystal id 1, crystal id 2, TOF bin
+    tof: tuple              # (num_bins, tof_range_mm, fwhm_mm)
+    randoms_per_bin: float  # additive term per event (expected randoms per LOR and TOF bin)
+    n_iters: int
+    n_subsets: int
+
+
+def config3(seed: int = 3, n_events: int = 10_000_000, randoms_fraction: float = 0.2,
+            info: dict | None = None, shape=(200, 200, 96), voxel_mm=(2.0, 2.0, 2.0),
+            tof=(13, 650.0, 58.5)) -> PetWorkload:
+    """TOF listmode events of an ellipsoid phantom (semi-axes 150 x 100 x 80 mm with two
+    4:1 hot spheres) on a 600-crystal x 96-ring scanner of radius 400 mm: true events are
+    emission points drawn from the phantom with isotropic directions that hit the
+    scanner, their TOF bin drawn from the Gaussian TOF kernel around the emission point;
+    randoms are uniform crystal pairs with uniform TOF bins."""
+    info = dict(PET_INFO if info is None else info)
+    rng = np.random.default_rng(seed)
+    n_rand = int(n_events * randoms_fraction)
+    n_true = n_events - n_rand
+    R = info["radius"]
+    n_tr = info["NrCrystalsPerRing"]
+    n_ring = info["NrRings"]
+    dz = info["crystalAxialSpacing"]
+    z_half = (n_ring - 1) * dz / 2
+    nb, tof_range, fwhm = tof
+    bw = tof_range / nb
+    sig = fwhm / 2.355
+    chunks = []
+    got = 0
+    while got < n_true:
+        m = 2 * (n_true - got) + 1000
+        # emission points: ellipsoid with two hot spheres (rejection sampling by activity)
+        p = rng.uniform(-1, 1, (m, 3)) * np.array([150.0, 100.0, 80.0])
+        inside = (p[:, 0] / 150) ** 2 + (p[:, 1] / 100) ** 2 + (p[:, 2] / 80) ** 2 <= 1
+        hot = ((p[:, 0] - 50) ** 2 + p[:, 1] ** 2 + p[:, 2] ** 2 <= 25.0 ** 2) | \
+              ((p[:, 0] + 60) ** 2 + (p[:, 1] - 30) ** 2 + (p[:, 2] - 20) ** 2 <= 15.0 ** 2)
+        act = np.where(hot, 4.0, 1.0) * inside
+        keep = rng.uniform(0, 4.0, m) < act
+        p = p[keep]
+        u = rng.normal(size=(len(p), 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        # intersections with the cylinder x^2 + y^2 = R^2
+        a = u[:, 0] ** 2 + u[:, 1] ** 2
+        b = 2 * (p[:, 0] * u[:, 0] + p[:, 1] * u[:, 1])
+        c = p[:, 0] ** 2 + p[:, 1] ** 2 - R ** 2
+        disc = np.sqrt(np.maximum(b * b - 4 * a * c, 0))
+        t1 = (-b - disc) / (2 * a + 1e-30)
+        t2 = (-b + disc) / (2 * a + 1e-30)
+        q1 = p + t1[:, None] * u
+        q2 = p + t2[:, None] * u
+        ok = (np.abs(q1[:, 2]) <= z_half) & (np.abs(q2[:, 2]) <= z_half) & (a > 1e-6)
+        p, q1, q2 = p[ok], q1[ok], q2[ok]
+
+        def crystal(q):
+            phi = np.arctan2(q[:, 1], q[:, 0]) % (2 * np.pi)
+            tr = np.rint(phi / (2 * np.pi / n_tr)).astype(np.int64) % n_tr
+            ring = np.clip(np.rint((z_half - q[:, 2]) / dz).astype(np.int64), 0, n_ring - 1)
+            return ring * n_tr + tr
+
+        i1, i2 = crystal(q1), crystal(q2)
+        # TOF: signed distance of the emission point from the LOR centre towards crystal 2
+        mid = (q1 + q2) / 2
+        d = q2 - q1
+        s = np.einsum("ij,ij->i", p - mid, d / np.linalg.norm(d, axis=1, keepdims=True))
+        s += rng.normal(0, sig, len(s))
+        tb = np.clip(np.rint(s / bw).astype(np.int64) + (nb - 1) // 2, 0, nb - 1)
+        good = i1 != i2
+        chunks.append(np.stack([i1[good], i2[good], tb[good]], 1))
+        got += int(good.sum())
+    trues = np.concatenate(chunks)[:n_true]
+    ri = rng.integers(0, n_tr * n_ring, n_rand)
+    rj = rng.integers(0, n_tr * n_ring - 1, n_rand)
+    rj = rj + (rj >= ri)
+    rt = rng.integers(0, nb, n_rand)
+    randoms = np.stack([ri, rj, rt], 1)
+    ev = np.concatenate([trues, randoms])
+    ev = ev[rng.permutation(len(ev))]
+    n_det = n_tr * n_ring
+    per_bin = n_rand / (n_det * (n_det - 1) / 2 * nb)
+    return PetWorkload(f"pet_lm_tof_{shape[0]}x{shape[1]}x{shape[2]}_{n_events // 1_000_000}M",
+                       shape, voxel_mm, info, ev, tof, per_bin, 2, 20)
+
+
+def build_pet_system_matrix(w: PetWorkload, compute_sensitivity: bool = False):
+    from .metadata import ObjectMeta
+    from .metadata.PET import PETLMProjMeta, PETTOFMeta
+    from .projectors.PET import PETLMSystemMatrix
+    nb, rng_mm, fwhm = w.tof
+    pm = PETLMProjMeta(torch.as_tensor(w.events), info=w.info,
+                       tof_meta=PETTOFMeta(nb, rng_mm, fwhm))
+    return PETLMSystemMatrix(ObjectMeta(list(w.voxel_mm), w.shape), pm,
+                             compute_sensitivity=compute_sensitivity)
