@@ -23,7 +23,7 @@ static bool b1_fixed(int K, int N, int Zt);
 
 #ifdef GB_PHASE_TIMING
 // Per-CTA cycle counts of k_b1_psf (diagnostic builds only): [1] phase 1 (S load),
-// [2] y blur, [3] z blur + W store, [4] planes, [5] total.
+// [2] y blur, [3] z blur + W store, [4] planes, [5] total, [6] rows, [7] rows x taps.
 __device__ unsigned long long g_b1_phase_cycles[4096 * 8];
 #define GB_B1T(k, v)                            \
     do {                                        \
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(512, 1)
     int2 *wr = g.wrange + (size_t)slot * g.Lp;
     int parity = 0;
 #ifdef GB_PHASE_TIMING
-    unsigned long long tacc[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const long long t_start = clock64();
 #endif
     long long t0 = GB_B1NOW();
@@ -166,6 +166,8 @@ __global__ void __launch_bounds__(512, 1)
             blur_first<K, KK1, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
         else
             blur_first<K, K, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        GB_B1T(6, rb - ra + 1);
+        GB_B1T(7, (rb - ra + 1) * (tier == 0 ? KK0 : (tier == 1 ? KK1 : K)));
         __syncthreads();
         {
             long long t1 = GB_B1NOW();
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(512, 1)
 #ifdef GB_PHASE_TIMING
     if (threadIdx.x == 0 && blockIdx.x < 4096) {
         tacc[5] = clock64() - t_start;
-        for (int k = 0; k < 6; k++)
+        for (int k = 0; k < 8; k++)
             g_b1_phase_cycles[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
     }
 #endif
@@ -253,6 +255,10 @@ __global__ void __launch_bounds__(512, 1)
 #ifdef GB_PHASE_TIMING
 extern "C" int gb_debug_b1_phase_cycles(unsigned long long *out, int n) {
     return (int)cudaMemcpyFromSymbol(out, g_b1_phase_cycles, sizeof(unsigned long long) * (size_t)n);
+}
+extern "C" int gb_debug_b1_phase_reset(void) {
+    static unsigned long long zero[4096 * 8];
+    return (int)cudaMemcpyToSymbol(g_b1_phase_cycles, zero, sizeof(zero));
 }
 #endif
 

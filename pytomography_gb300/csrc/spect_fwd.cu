@@ -21,7 +21,7 @@ namespace gb {
 #ifdef GB_PHASE_TIMING
 // Per-CTA cycle counts of the forward kernel's phases (diagnostic builds only):
 // [0] waits for the attenuation copy, [1] phase 1, [2] phase 2, [3] phase 3,
-// [4] planes processed, [5] total.
+// [4] planes processed, [5] total, [6] rows sampled, [7] output rows x taps.
 __device__ unsigned long long g_fwd_phase_cycles[4096 * 8];
 #define GB_T(k, v)                                              \
     do {                                                        \
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(512, 1)
     int parity = 0;
     unsigned phase = 0;
 #ifdef GB_PHASE_TIMING
-    unsigned long long tacc[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const long long t_start = clock64();
 #endif
     long long t0 = GB_NOW();
@@ -280,6 +280,8 @@ __global__ void __launch_bounds__(512, 1)
             blur_first<K, KK1, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
         else
             blur_first<K, K, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        GB_T(6, rb - ra + 1);
+        GB_T(7, (b_hi - b_lo) * OB * (tier == 0 ? KK0 : (tier == 1 ? KK1 : K)));
         __syncthreads();
         {
             long long t1 = GB_NOW();
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(512, 1)
 #ifdef GB_PHASE_TIMING
     if (threadIdx.x == 0 && blockIdx.x < 4096) {
         tacc[5] = clock64() - t_start;
-        for (int k = 0; k < 6; k++) g_fwd_phase_cycles[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
+        for (int k = 0; k < 8; k++) g_fwd_phase_cycles[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
     }
 #endif
     // partial ray sums of this item
@@ -505,6 +507,10 @@ cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, cons
 extern "C" int gb_debug_fwd_phase_cycles(unsigned long long *out, int n) {
     return (int)cudaMemcpyFromSymbol(out, g_fwd_phase_cycles,
                                      sizeof(unsigned long long) * (size_t)n);
+}
+extern "C" int gb_debug_phase_reset(void) {
+    static unsigned long long zero[4096 * 8];
+    return (int)cudaMemcpyToSymbol(g_fwd_phase_cycles, zero, sizeof(zero));
 }
 #endif
 

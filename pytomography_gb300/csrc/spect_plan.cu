@@ -53,6 +53,8 @@ struct gb_spect_plan {
     float *d_taps_r = nullptr, *d_taps_z = nullptr, *d_A = nullptr;
     signed char *d_tier = nullptr;
     int *d_group = nullptr;
+    std::vector<signed char> h_tier;  // tap tier per (PSF group, plane)
+    std::vector<int> h_group;         // PSF group per angle
     // angle lists: [all][subset 0][subset 1]..., with their work items
     int *d_alist = nullptr;
     int4 *d_items = nullptr;
@@ -125,26 +127,36 @@ static bool host_plane_rows(const gb_spect_plan *p, int a, int xp, int ylo, int 
     return ra <= rb;
 }
 
-// Estimated work of every plane of angle a: forward (rows sampled + 2 x rows blurred)
-// or B1 (2 x rows blurred).
+// Estimated cost (SM cycles) of every plane of angle a, a linear model fitted to
+// per-CTA cycle counts of both kernels on GB300 over object sizes 64-128 and 60-120
+// angles: a fixed cost per occupied plane (barriers, pipeline drain), a cost per sampled
+// row and a cost per blurred output row and tap (the plane's tap tier sets the taps).
+//   forward: 6100 + 158 rows + 4.4 (output rows x taps)
+//   B1:      3700 + 113 rows + 2.5 (rows x taps)
+// A plane that no sample reaches costs about one plane-support test.
 static std::vector<double> plane_work(const gb_spect_plan *p, int a, bool fwd) {
-    std::vector<double> w(p->Lp, 1.0);
-    const int H = p->H;
+    std::vector<double> w(p->Lp, 200.0);
+    const int H = p->H, K = p->dev.K;
     const int ylo = std::max(0, p->pad - H), yhi = std::min(p->Lp, p->pad + p->N + H);
+    const int grp = p->h_group.empty() ? 0 : p->h_group[a];
     for (int xp = 0; xp < p->Lp; xp++) {
         int ra, rb;
         if (!host_plane_rows(p, a, xp, ylo, yhi, fwd ? 0.5 : 1.5, ra, rb)) continue;
+        const int tier = p->h_tier.empty() ? 2 : p->h_tier[(size_t)grp * p->Lp + xp];
+        const double kk = 2 * tier_half(K, tier) + 1;
+        const double rows = rb - ra + 1;
         if (fwd) {
-            int o = std::min(p->N, rb + H - p->pad + 1) - std::max(0, ra - H - p->pad);
-            w[xp] = 4.0 + (rb - ra + 1) + 2.0 * std::max(0, o);
+            const int o = std::min(p->N, rb + H - p->pad + 1) - std::max(0, ra - H - p->pad);
+            w[xp] = 6100.0 + 158.0 * rows + 4.4 * kk * std::max(0, o);
         } else {
-            w[xp] = 4.0 + 2.0 * (rb - ra + 1);
+            w[xp] = 3700.0 + 113.0 * rows + 2.5 * kk * rows;
         }
     }
     return w;
 }
 
-// Split [0, Lp) into c contiguous plane ranges of about equal work.
+// Split [0, Lp) into c contiguous plane ranges of about equal work: each boundary is put
+// where the running sum comes closest to its share.
 static void split_planes(const std::vector<double> &w, int c, int slot,
                          std::vector<int4> &out) {
     const int L = (int)w.size();
@@ -157,8 +169,9 @@ static void split_planes(const std::vector<double> &w, int c, int slot,
         int end = L;
         if (k < c) {
             const double target = total * k / c;
-            while (x < L && acc + w[x] <= target) acc += w[x++];
-            end = x;
+            while (x < L - (c - k) && acc + 0.5 * w[x] <= target) acc += w[x++];
+            end = std::max(x, prev + 1);
+            while (x < end) acc += w[x++];
         }
         out.push_back(make_int4(slot, prev, end, 0));
         prev = end;
@@ -172,13 +185,38 @@ static int nopsf_chunks(const gb_spect_plan *p, int n_sel) {
     return std::max(1, std::min(c, std::max(1, p->Lp / 4)));
 }
 
-// Per-angle chunk counts so that n angles x chunks x z-slabs is about one wave.
-static std::vector<int> chunk_counts(const gb_spect_plan *p, int n, int zslabs) {
-    int T = std::max(n, p->sm_count / std::max(1, zslabs));
-    std::vector<int> c(n, T / n);
-    for (int i = 0; i < T % n; i++) c[i]++;
-    for (int &v : c) v = std::max(1, std::min(v, std::max(1, p->Lp / 4)));
+// Per-angle chunk counts: about one wave of items (n angles x chunks x z-slabs), each
+// angle's share proportional to its estimated work (largest remainder), at least one.
+static std::vector<int> chunk_counts(const gb_spect_plan *p, const std::vector<double> &work,
+                                     int zslabs) {
+    const int n = (int)work.size();
+    const int T = std::max(n, p->sm_count / std::max(1, zslabs));
+    const int cmax = std::max(1, p->Lp / 4);
+    double total = 0;
+    for (double v : work) total += v;
+    std::vector<int> c(n, 1);
+    if (total <= 0) return c;
+    std::vector<std::pair<double, int>> rem;
+    int used = 0;
+    for (int i = 0; i < n; i++) {
+        const double share = T * work[i] / total;
+        c[i] = std::max(1, std::min(cmax, (int)share));
+        used += c[i];
+        rem.push_back({share - (int)share, i});
+    }
+    std::sort(rem.begin(), rem.end(), [](auto &a, auto &b) { return a.first > b.first; });
+    for (size_t k = 0; used < T && k < rem.size(); k++)
+        if (c[rem[k].second] < cmax) {
+            c[rem[k].second]++;
+            used++;
+        }
     return c;
+}
+
+static double sum_of(const std::vector<double> &v) {
+    double t = 0;
+    for (double x : v) t += x;
+    return t;
 }
 
 static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
@@ -216,7 +254,9 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
         L.fitem_off = (int)items.size();
         L.ioff_off = (int)ioff.size();
         if (psf) {
-            std::vector<int> cnt = chunk_counts(p, L.n, zs_f);
+            std::vector<double> wa(L.n);
+            for (int i = 0; i < L.n; i++) wa[i] = sum_of(wf[l[i]]);
+            std::vector<int> cnt = chunk_counts(p, wa, zs_f);
             for (int i = 0; i < L.n; i++) {
                 ioff.push_back((int)items.size() - L.fitem_off);
                 split_planes(wf[l[i]], cnt[i], i, items);
@@ -237,7 +277,9 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
             int na = std::min(p->G, L.n - a0);
             L.gitem_off.push_back((int)items.size());
             if (psf) {
-                std::vector<int> cnt = chunk_counts(p, na, zs_b);
+                std::vector<double> wa(na);
+                for (int i = 0; i < na; i++) wa[i] = sum_of(wb[l[a0 + i]]);
+                std::vector<int> cnt = chunk_counts(p, wa, zs_b);
                 for (int i = 0; i < na; i++) split_planes(wb[l[a0 + i]], cnt[i], i, items);
             }
             L.n_gitems.push_back((int)items.size() - L.gitem_off.back());
@@ -399,6 +441,7 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     FAIL_CUDA(cudaMemcpy(p->d_theta_bwd, d->theta_bwd, 6 * n * sizeof(float), cudaMemcpyHostToDevice));
     std::vector<int> grp(n, 0);
     if (psf) std::copy(d->psf_group, d->psf_group + n, grp.begin());
+    p->h_group = grp;
     FAIL_CUDA(cudaMalloc(&p->d_group, n * sizeof(int)));
     FAIL_CUDA(cudaMemcpy(p->d_group, grp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     if (psf) {
@@ -435,6 +478,7 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
                 tier[(size_t)gi * Lp + x] =
                     h <= tier_half(K, 0) ? 0 : (h <= tier_half(K, 1) ? 1 : 2);
             }
+        p->h_tier = tier;
         FAIL_CUDA(cudaMalloc(&p->d_tier, tier.size()));
         FAIL_CUDA(cudaMemcpy(p->d_tier, tier.data(), tier.size(), cudaMemcpyHostToDevice));
         FAIL_CUDA(cudaMalloc(&p->d_taps_r, tr.size() * sizeof(float)));
