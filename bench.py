@@ -8,6 +8,9 @@ angles over 360 deg at 22 cm, PSF sigma(d) = 0.03 d + 0.11 cm, Poisson projectio
   value    : fused sub-iterations (forward with ratio epilogue, back-projection with
              fused update) replayed from captured CUDA graphs, inputs resident in HBM
   plain    : the per-call drop-in path (forward, torch ratio, backward, torch update)
+  torch_reference : the reference's per-call GPU sequence restated in plain PyTorch
+             float32 (per angle: pad, grid_sample rotation of object and mu, cumsum
+             attenuation, grouped conv1d PSF, sum; tests/torch_reference.py)
   e2e      : OSEM(likelihood)(4, 10) through the public API from host tensors
              (system matrix construction, H2D of projections and mu, normalisation,
              40 sub-iterations, D2H of the result), reported per sub-iteration
@@ -326,6 +329,20 @@ def run_serving(args, dev):
     e1.record()
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1) / n_plain
+    # the reference's per-call GPU sequence in plain PyTorch: one round over all
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from torch_reference import TorchReferenceProjector
+    refs = [TorchReferenceProjector(H) for H in Hs]
+    tr = [torch.ones(w.shape, device=dev) for w in ws]
+    tr[0] = refs[0].osem_subiteration(tr[0], gs[0], None, liks[0]._get_normBP(0), 0)
+    torch.cuda.synchronize()
+    e0.record()
+    for i in range(R):
+        tr[i] = refs[i].osem_subiteration(tr[i], gs[i], None, liks[i]._get_normBP(1), 1)
+    e1.record()
+    torch.cuda.synchronize()
+    torch_ref_ms = e0.elapsed_time(e1)
+    del refs, tr
     batch = BatchedOSEM([PoissonLogLikelihood(H, g) for H, g in zip(Hs, gs)], n_subsets=10)
     batch.capture()
     for k in range(max(3, args.warmup)):
@@ -348,7 +365,11 @@ def run_serving(args, dev):
                        "sizes": [w.shape[0] for w in ws],
                        "angles": [len(w.angles) for w in ws]},
             "plain": {"value": R * 1000.0 / plain_ms, "ms_per_step": plain_ms},
-            "batched_vs_plain": plain_ms / batch_ms}
+            "batched_vs_plain": plain_ms / batch_ms,
+            "torch_reference": {"value": R * 1000.0 / torch_ref_ms, "ms_per_step": torch_ref_ms,
+                                "what": "the reference's per-call GPU sequence restated in "
+                                        "plain PyTorch float32, one round of 32"},
+            "batched_vs_torch_reference": torch_ref_ms / batch_ms}
     print(json.dumps(line))
 
 
@@ -431,6 +452,23 @@ def main():
     e1.record()
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1) / n_plain
+
+    # ---- the reference's per-call GPU sequence in plain PyTorch (context line)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from torch_reference import TorchReferenceProjector
+    R = TorchReferenceProjector(H)
+    ft = torch.ones(w.shape, device=dev)
+    for k in range(2):
+        ft = R.osem_subiteration(ft, g, None, nbps[k], k)
+    torch.cuda.synchronize()
+    n_tr = 5
+    e0.record()
+    for k in range(n_tr):
+        ft = R.osem_subiteration(ft, g, None, nbps[k % n_sub], k % n_sub)
+    e1.record()
+    torch.cuda.synchronize()
+    torch_ref_ms = e0.elapsed_time(e1) / n_tr
+    del R, ft
 
     # ---- fused sub-iterations, one CUDA graph per subset
     f.fill_(1.0)
@@ -538,6 +576,11 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single"},
             "plain": {"value": 1000.0 / plain_ms, "unit": "subiter/s", "ms_per_step": plain_ms},
             "fused_vs_plain": plain_ms / fused_ms,
+            "torch_reference": {"value": 1000.0 / torch_ref_ms, "unit": "subiter/s",
+                                "ms_per_step": torch_ref_ms,
+                                "what": "the reference's per-call GPU sequence restated in "
+                                        "plain PyTorch float32 (tests/torch_reference.py)"},
+            "fused_vs_torch_reference": torch_ref_ms / fused_ms,
             "e2e": {"value": e2e_subiter, "unit": "subiter/s",
                     "h2d_bytes_per_step": int((g_host.numel() + mu_host.numel()) * 4
                                               / (w.n_iters * w.n_subsets)),

@@ -87,6 +87,27 @@ gb_status gb_spect_set_subsets(gb_spect_plan *plan, int32_t n_subsets);
 /* Number of angles in a subset (-1 = all angles). */
 int32_t gb_spect_subset_size(const gb_spect_plan *plan, int32_t subset);
 
+/* Tile configuration of a plan's PSF kernels.  Plan creation picks the widest tiles that
+ * fit shared memory; gb_spect_autotune times candidates on the device and keeps the
+ * fastest.  No counterpart in the reference (which has no device code). */
+typedef struct gb_spect_tuning {
+    int32_t fwd_tpb;   /* threads per forward CTA: 512 (one CTA per SM) or 256 (two) */
+    int32_t fwd_zt;    /* forward z-slab width; 0 = the widest that fits */
+    int32_t fwd_items; /* forward work items per resident CTA slot and z slab: 1 or 2 */
+    int32_t b1_zt;     /* back-projection (rotated frame) z-slab width; 0 = widest */
+    int32_t b1_items;  /* back-projection work items per SM and z slab: 1 or 2 */
+} gb_spect_tuning;
+gb_status gb_spect_get_tuning(const gb_spect_plan *plan, gb_spect_tuning *out);
+/* Apply a tuning (rebuilds the work lists of the current subsets; may allocate: call at
+ * set-up, outside stream capture).  GB_ERR_UNSUPPORTED when a tile does not fit. */
+gb_status gb_spect_set_tuning(gb_spect_plan *plan, const gb_spect_tuning *tuning);
+/* Time the candidate tunings on `subset` (reps launches each, on a temporary object of
+ * ones), apply the fastest forward and back-projection tiles and return them in *out
+ * (may be NULL).  Allocates temporaries: call at set-up, outside stream capture.  A plan
+ * without PSF has nothing to tune and returns its tuning unchanged. */
+gb_status gb_spect_autotune(gb_spect_plan *plan, int32_t subset, int32_t reps,
+                            gb_spect_tuning *out, gb_stream_t stream);
+
 /* Forward projection H_m f -> proj [n_sel][ny][nz] (device).
  * Replaces SPECTSystemMatrix.forward (spect_system_matrix.py:120-157).
  * subset = -1 projects every angle. */

@@ -33,6 +33,14 @@ class SpectDesc(ctypes.Structure):
     ]
 
 
+class SpectTuning(ctypes.Structure):
+    _fields_ = [("fwd_tpb", c_int), ("fwd_zt", c_int), ("fwd_items", c_int), ("b1_zt", c_int),
+                ("b1_items", c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 class RdpDesc(ctypes.Structure):
     _fields_ = [("beta", c_float), ("gamma", c_float), ("delta", c_float),
                 ("fov_scale", c_void_p)]
@@ -61,6 +69,9 @@ SIGNATURES = [
     ("gb_spect_set_subsets", c_int, [c_void_p, c_int]),
     ("gb_spect_device_status", c_int, [c_void_p, ctypes.POINTER(c_int)]),
     ("gb_spect_subset_size", c_int, [c_void_p, c_int]),
+    ("gb_spect_get_tuning", c_int, [c_void_p, ctypes.POINTER(SpectTuning)]),
+    ("gb_spect_set_tuning", c_int, [c_void_p, ctypes.POINTER(SpectTuning)]),
+    ("gb_spect_autotune", c_int, [c_void_p, c_int, c_int, ctypes.POINTER(SpectTuning), c_void_p]),
     ("gb_spect_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("gb_spect_backward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
     ("gb_spect_osem_step", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,

@@ -5,7 +5,8 @@ count, PSF table and attenuation factors).  For every subset index ``k`` the fus
 sub-iterations of all reconstructions are recorded once into a CUDA graph and the
 graphs are replayed for every iteration; inside a graph the reconstructions are spread
 over several streams so that their kernels run concurrently and small problems fill the
-GPU together.  The plain alternative runs the same reconstructions one after another
+GPU together.  Each plan's kernel tiles are picked by the autotuner (timed once per
+geometry and process).  The plain alternative runs the same reconstructions one after another
 through the per-call drop-in path.
 
 Usage::
@@ -23,7 +24,7 @@ from .projectors.SPECT import SPECTSystemMatrix
 
 class BatchedOSEM:
     def __init__(self, likelihoods, n_subsets: int, object_initial=None, n_streams: int = 4,
-                 use_graphs: bool = True) -> None:
+                 use_graphs: bool = True, autotune: bool = True) -> None:
         if not likelihoods:
             raise ValueError("no reconstructions")
         for lik in likelihoods:
@@ -44,6 +45,8 @@ class BatchedOSEM:
                 f = sm._get_object_initial(sm.device).to(torch.float32).contiguous()
             self.objects.append(f)
             lik._set_n_subsets(self.n_subsets)
+            if autotune:  # tile shapes per geometry, timed once per process
+                sm.autotune(0 if self.n_subsets > 1 else None)
             lik.projections = lik.projections.to(sm.device, torch.float32).contiguous()
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max(1, n_streams))]
         self._graphs = None

@@ -70,13 +70,17 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 //   taps [2][2][K]: double-buffered y / z taps of the current plane
 //   one mbarrier for the TMA copies
 // Per plane only the rows the rotated object square can reach are sampled / blurred.
-// FIXED: the tile fits 128 output rows and a 128-wide z slab, so the shared-memory row
-// strides are compile-time constants (immediate-offset loads in the blur loops).
-template <int K, bool VEC, bool FIXED>
-__global__ void __launch_bounds__(512, 1)
+// FIXED: the tile fits 128 output rows and a z slab of at most ZW (128 for 512-thread
+// CTAs, 64 for 256-thread CTAs), so the shared-memory row strides are compile-time
+// constants (immediate-offset loads in the blur loops).
+// TPB: 512 threads and one CTA per SM, or 256 threads with a half-width z slab and two
+// CTAs per SM (one CTA's gathers overlap the other's blur arithmetic).
+template <int K, bool VEC, bool FIXED, int TPB>
+__global__ void __launch_bounds__(TPB, 512 / TPB)
     k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
               const int4 *__restrict__ items, int Zt, float *__restrict__ partials) {
     constexpr int H = K / 2;
+    constexpr int ZW = TPB >= 512 ? 128 : 64;
     constexpr int HP = (H + 3) / 4 * 4;
     constexpr int OB = (K <= 31) ? 8 : 4;  // outputs per task
     constexpr int NACC = 32 / OB;          // phase-3 tasks per thread
@@ -88,7 +92,7 @@ __global__ void __launch_bounds__(512, 1)
     const int Zc = min(Zt, nz - z0);
     const int N8 = (N + OB - 1) / OB * OB;
     const int Z8 = (Zc + OB - 1) / OB * OB;
-    constexpr int SC_FIX = 128 + 2 * HP, TS_FIX = 129;
+    constexpr int SC_FIX = ZW + 2 * HP, TS_FIX = 129;
     const int SC = FIXED ? SC_FIX : Z8 + 2 * HP, SR = N8 + 2 * H;
     const int TS = FIXED ? TS_FIX : N8 + 1, TR = Z8 + 2 * HP;
     extern __shared__ __align__(128) float sm[];
@@ -97,7 +101,7 @@ __global__ void __launch_bounds__(512, 1)
     float *tp = Tt + TR * TS;
     unsigned long long *bar =
         reinterpret_cast<unsigned long long *>(tp + ((4 * K + 1) & ~1));
-    for (int i = threadIdx.x; i < SR * SC + TR * TS; i += blockDim.x) sm[i] = 0.f;
+    for (int i = threadIdx.x; i < SR * SC + TR * TS; i += TPB) sm[i] = 0.f;
 
     float th[6];
 #pragma unroll
@@ -111,7 +115,8 @@ __global__ void __launch_bounds__(512, 1)
     const int cz_lo = zv_lo - z0 + HP, cz_hi = zv_hi - z0 + HP;
     const int ncol = cz_hi - cz_lo;
     const int ylo = max(0, g.pad - H), yhi = min(g.Lp, g.pad + N + H);  // sampled rows
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int nwarp = TPB / 32;
     const int zq_lo = zv_lo & ~3, zq_hi = (zv_hi + 3) & ~3;  // z quads (vector path)
     const int nq = (zq_hi - zq_lo) >> 2;
     const unsigned row_bytes = (unsigned)(zq_hi - zq_lo) * 4u;
@@ -132,7 +137,7 @@ __global__ void __launch_bounds__(512, 1)
                 tz[k] = warp + nwarp * (k / n_yc);
                 if (ty[k] >= N8 || k / n_yc >= NACC / n_yc) tz[k] = 1 << 20;  // no task
             } else {
-                const int task = threadIdx.x + k * blockDim.x;
+                const int task = threadIdx.x + k * TPB;
                 ty[k] = task % N8;
                 tz[k] = task / N8;
             }
@@ -247,7 +252,7 @@ __global__ void __launch_bounds__(512, 1)
                 }
             }
         } else {
-            for (int i = threadIdx.x; i < (yhi - ylo) * ncol; i += blockDim.x) {
+            for (int i = threadIdx.x; i < (yhi - ylo) * ncol; i += TPB) {
                 int y = ylo + i / ncol, c = cz_lo + i % ncol;
                 int z = z0 - HP + c;
                 float v = 0.f;
@@ -417,67 +422,64 @@ __global__ void k_reduce(const int *__restrict__ ioff, int NZ, const float *__re
 }
 
 // ------------------------------------------------------------- launchers
-static bool fwd_fixed(int K, int N, int Zt) {
+static bool fwd_fixed(int K, int N, int Zt, int tpb) {
     int OB = (K <= 31) ? 8 : 4;
-    return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= 128;
+    return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= (tpb >= 512 ? 128 : 64);
 }
 
-size_t fwd_psf_smem_bytes(int K, int N, int Zt) {
+size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb) {
     int H = K / 2, HP = (H + 3) / 4 * 4, OB = (K <= 31) ? 8 : 4;
     int N8 = (N + OB - 1) / OB * OB;
     int Z8 = (Zt + OB - 1) / OB * OB;
-    const bool fx = fwd_fixed(K, N, Zt);
-    size_t SC = fx ? 128 + 2 * HP : Z8 + 2 * HP, TS = fx ? 129 : N8 + 1;
+    const bool fx = fwd_fixed(K, N, Zt, tpb);
+    const int ZW = tpb >= 512 ? 128 : 64;
+    size_t SC = fx ? ZW + 2 * HP : Z8 + 2 * HP, TS = fx ? 129 : N8 + 1;
     return sizeof(float) * ((size_t)(N8 + 2 * H) * SC + (size_t)(Z8 + 2 * HP) * TS +
                             ((4 * K + 1) & ~1)) +
            sizeof(unsigned long long);
 }
 
-template <int K>
-static cudaError_t launch_fwd_psf_k(const SpectDev &g, const float *f, const int *alist,
+template <int K, int TPB>
+static cudaError_t launch_fwd_psf_t(const SpectDev &g, const float *f, const int *alist,
                                     const int4 *items, int n_items, int Zt, float *partials,
                                     cudaStream_t st) {
-    size_t smem = fwd_psf_smem_bytes(K, g.N, Zt);
+    size_t smem = fwd_psf_smem_bytes(K, g.N, Zt, TPB);
     dim3 grid(n_items, (g.nz + Zt - 1) / Zt);
-    const bool fx = fwd_fixed(K, g.N, Zt);
+    const bool fx = fwd_fixed(K, g.N, Zt, TPB);
     if (g.nz % 4 == 0) {
         if (fx)
-            k_fwd_psf<K, true, true><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+            k_fwd_psf<K, true, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
         else
-            k_fwd_psf<K, true, false><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+            k_fwd_psf<K, true, false, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
     } else {
         if (fx)
-            k_fwd_psf<K, false, true><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+            k_fwd_psf<K, false, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
         else
-            k_fwd_psf<K, false, false><<<grid, 512, smem, st>>>(g, f, alist, items, Zt, partials);
+            k_fwd_psf<K, false, false, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt,
+                                                                    partials);
     }
     return cudaGetLastError();
 }
 
-template <int K>
-static cudaError_t setup_fwd_k(size_t smem) {
-    cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_fwd_psf<K, true, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-        return e;
-    if ((e = cudaFuncSetAttribute(k_fwd_psf<K, true, false>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-        return e;
-    if ((e = cudaFuncSetAttribute(k_fwd_psf<K, false, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
-        return e;
-    return cudaFuncSetAttribute(k_fwd_psf<K, false, false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int K, int TPB>
+static cudaError_t setup_fwd_t(size_t smem) {
+    const void *fns[4] = {(const void *)k_fwd_psf<K, true, true, TPB>,
+                          (const void *)k_fwd_psf<K, true, false, TPB>,
+                          (const void *)k_fwd_psf<K, false, true, TPB>,
+                          (const void *)k_fwd_psf<K, false, false, TPB>};
+    for (const void *fn : fns) {
+        cudaError_t e =
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
-cudaError_t setup_fwd(int K, size_t smem) {
+cudaError_t setup_fwd(int K, size_t smem, int tpb) {
     switch (K) {
 #define GB_SETUP_CASE(KK) \
     case KK:              \
-        return setup_fwd_k<KK>(smem);
+        return tpb >= 512 ? setup_fwd_t<KK, 512>(smem) : setup_fwd_t<KK, 256>(smem);
         GB_FOR_EACH_K(GB_SETUP_CASE)
 #undef GB_SETUP_CASE
         default:
@@ -486,16 +488,18 @@ cudaError_t setup_fwd(int K, size_t smem) {
 }
 
 cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, const int4 *items,
-                       int n_items, int Zt, float *partials, cudaStream_t st) {
+                       int n_items, int Zt, int tpb, float *partials, cudaStream_t st) {
     if (!g.psf) {
         dim3 grid(n_items, (g.N * g.nz + 255) / 256);
         k_fwd_nopsf<<<grid, 256, 0, st>>>(g, f, alist, items, partials);
         return cudaGetLastError();
     }
     switch (g.K) {
-#define GB_FWD_CASE(KK) \
-    case KK:            \
-        return launch_fwd_psf_k<KK>(g, f, alist, items, n_items, Zt, partials, st);
+#define GB_FWD_CASE(KK)                                                                      \
+    case KK:                                                                                 \
+        return tpb >= 512                                                                    \
+                   ? launch_fwd_psf_t<KK, 512>(g, f, alist, items, n_items, Zt, partials, st) \
+                   : launch_fwd_psf_t<KK, 256>(g, f, alist, items, n_items, Zt, partials, st);
         GB_FOR_EACH_K(GB_FWD_CASE)
 #undef GB_FWD_CASE
         default:

@@ -18,17 +18,18 @@ inline int psf_bucket(int k) {
     return -1;
 }
 
-size_t fwd_psf_smem_bytes(int K, int N, int Zt);
+// tpb: threads per forward CTA, 512 (one CTA per SM) or 256 (two CTAs per SM)
+size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb);
 size_t b1_psf_smem_bytes(int K, int N, int Zt);
 // Raise the dynamic shared-memory limit of the PSF kernels (done once at plan creation,
 // outside any stream capture).
-cudaError_t setup_fwd(int K, size_t smem);
+cudaError_t setup_fwd(int K, size_t smem, int tpb);
 cudaError_t setup_b1(int K, size_t smem);
 
 // Work items (int4: slot, first plane, end plane, unused) split each angle's planes
 // into ranges of about equal work; partial sums are indexed by item.
 cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, const int4 *items,
-                       int n_items, int Zt, float *partials, cudaStream_t st);
+                       int n_items, int Zt, int tpb, float *partials, cudaStream_t st);
 // ioff[slot] .. ioff[slot+1]: the items of a slot
 cudaError_t launch_reduce(int n_slots, const int *ioff, int NZ, const float *partials, float *out,
                           int ratio, const float *gproj, const float *sadd, const int *alist,
@@ -54,6 +55,7 @@ struct FwdArgs {
     int n_items;
     const int *ioff;
     int Zt;
+    int tpb;
 };
 bool plan_forward_args(const gb_spect_plan *p, int subset, FwdArgs *a);
 

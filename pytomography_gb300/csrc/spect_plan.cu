@@ -38,6 +38,17 @@ static size_t max_smem_optin() {
     return v > 0 ? (size_t)v : 227 * 1024;
 }
 
+// Shared memory one CTA may use when `per_sm` CTAs share an SM.
+static size_t smem_cap(int per_sm) {
+    if (per_sm <= 1) return max_smem_optin();
+    int dev = 0, sm = 0, res = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&res, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (sm <= 0) sm = 228 * 1024;
+    return std::min(max_smem_optin(), (size_t)(sm / per_sm - res));
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -77,6 +88,8 @@ struct gb_spect_plan {
     int2 *d_wrange = nullptr;
     int *d_err = nullptr;
     int Zt_fwd = 0, Zt_b1 = 0;
+    int fwd_tpb = 512;  // forward CTA size: 512 (one CTA per SM) or 256 (two per SM)
+    int fwd_items = 1, b1_items = 1;  // work items per resident CTA slot and z slab
 };
 
 static void free_plan(gb_spect_plan *p) {
@@ -188,9 +201,9 @@ static int nopsf_chunks(const gb_spect_plan *p, int n_sel) {
 // Per-angle chunk counts: about one wave of items (n angles x chunks x z-slabs), each
 // angle's share proportional to its estimated work (largest remainder), at least one.
 static std::vector<int> chunk_counts(const gb_spect_plan *p, const std::vector<double> &work,
-                                     int zslabs) {
+                                     int zslabs, int per_sm = 1) {
     const int n = (int)work.size();
-    const int T = std::max(n, p->sm_count / std::max(1, zslabs));
+    const int T = std::max(n, p->sm_count * per_sm / std::max(1, zslabs));
     const int cmax = std::max(1, p->Lp / 4);
     double total = 0;
     for (double v : work) total += v;
@@ -256,7 +269,7 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
         if (psf) {
             std::vector<double> wa(L.n);
             for (int i = 0; i < L.n; i++) wa[i] = sum_of(wf[l[i]]);
-            std::vector<int> cnt = chunk_counts(p, wa, zs_f);
+            std::vector<int> cnt = chunk_counts(p, wa, zs_f, (512 / p->fwd_tpb) * p->fwd_items);
             for (int i = 0; i < L.n; i++) {
                 ioff.push_back((int)items.size() - L.fitem_off);
                 split_planes(wf[l[i]], cnt[i], i, items);
@@ -279,7 +292,7 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
             if (psf) {
                 std::vector<double> wa(na);
                 for (int i = 0; i < na; i++) wa[i] = sum_of(wb[l[a0 + i]]);
-                std::vector<int> cnt = chunk_counts(p, wa, zs_b);
+                std::vector<int> cnt = chunk_counts(p, wa, zs_b, p->b1_items);
                 for (int i = 0; i < na; i++) split_planes(wb[l[a0 + i]], cnt[i], i, items);
             }
             L.n_gitems.push_back((int)items.size() - L.gitem_off.back());
@@ -327,20 +340,21 @@ static bool select_list(const gb_spect_plan *p, int subset, const int **alist, i
 }
 
 // z-slab width for the PSF kernels: the largest multiple of the output block that fits
-// shared memory (and, for the forward, the 32 accumulator registers per thread).
-static int choose_zt(int K, int N, int nz, bool fwd) {
+// shared memory (and, for the forward, the 32 accumulator registers per thread of a
+// `tpb`-thread CTA; with 256 threads two CTAs share an SM).
+static int choose_zt(int K, int N, int nz, bool fwd, int tpb = 512) {
     int OB = (K <= 31) ? 8 : 4;
-    size_t cap = max_smem_optin();
-    int best = OB;
+    size_t cap = fwd ? smem_cap(512 / tpb) : max_smem_optin();
+    int best = 0;
     for (int zt = OB; zt < nz + OB; zt += OB) {
         int z = std::min(zt, (nz + OB - 1) / OB * OB);
-        size_t sm = fwd ? fwd_psf_smem_bytes(K, N, z) : b1_psf_smem_bytes(K, N, z);
+        size_t sm = fwd ? fwd_psf_smem_bytes(K, N, z, tpb) : b1_psf_smem_bytes(K, N, z);
         if (sm > cap) break;
-        if (fwd) {  // phase-3 tasks of k_fwd_psf: 16 warps x (32 / OB) tasks per thread
+        if (fwd) {  // phase-3 tasks of k_fwd_psf: tpb / 32 warps x (32 / OB) tasks per thread
             const int N8 = (N + OB - 1) / OB * OB, NACC = 32 / OB, n_yc = (N8 + 31) / 32;
             if (n_yc <= NACC) {
-                if (z / OB > 16 * (NACC / n_yc)) break;
-            } else if ((long)N8 * (z / OB) > 512L * NACC) {
+                if (z / OB > (tpb / 32) * (NACC / n_yc)) break;
+            } else if ((long)N8 * (z / OB) > (long)tpb * NACC) {
                 break;
             }
         }
@@ -487,15 +501,14 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
         FAIL_CUDA(cudaMemcpy(p->d_taps_z, tz.data(), tz.size() * sizeof(float), cudaMemcpyHostToDevice));
         p->Zt_fwd = choose_zt(K, p->N, p->nz, true);
         p->Zt_b1 = choose_zt(K, p->N, p->nz, false);
-        size_t sf = fwd_psf_smem_bytes(K, p->N, p->Zt_fwd), sb = b1_psf_smem_bytes(K, p->N, p->Zt_b1);
-        if (sf > max_smem_optin() || sb > max_smem_optin()) {
-            set_error("PSF tiles need %zu / %zu bytes of shared memory (max %zu)", sf, sb,
-                      max_smem_optin());
+        if (!p->Zt_fwd || !p->Zt_b1) {
+            set_error("PSF tiles of %d taps at %d rows do not fit shared memory (max %zu)", K,
+                      p->N, max_smem_optin());
             free_plan(p);
             return GB_ERR_UNSUPPORTED;
         }
-        FAIL_CUDA(setup_fwd(K, sf));
-        FAIL_CUDA(setup_b1(K, sb));
+        FAIL_CUDA(setup_fwd(K, fwd_psf_smem_bytes(K, p->N, p->Zt_fwd, 512), 512));
+        FAIL_CUDA(setup_b1(K, b1_psf_smem_bytes(K, p->N, p->Zt_b1)));
     } else {
         p->Zt_fwd = p->Zt_b1 = p->nz;
     }
@@ -566,6 +579,56 @@ int32_t gb_spect_subset_size(const gb_spect_plan *p, int32_t subset) {
     return n;
 }
 
+gb_status gb_spect_get_tuning(const gb_spect_plan *p, gb_spect_tuning *out) {
+    clear_error();
+    GB_CHECK_ARG(p && out, "null argument");
+    out->fwd_tpb = p->fwd_tpb;
+    out->fwd_zt = p->Zt_fwd;
+    out->fwd_items = p->fwd_items;
+    out->b1_zt = p->Zt_b1;
+    out->b1_items = p->b1_items;
+    return GB_OK;
+}
+
+// Check a tuning against the plan's limits and fill in the z slabs left at 0.
+static gb_status resolve_tuning(const gb_spect_plan *p, gb_spect_tuning &t) {
+    const int K = p->dev.K, OB = (K <= 31) ? 8 : 4;
+    GB_CHECK_ARG(t.fwd_tpb == 512 || t.fwd_tpb == 256, "fwd_tpb must be 512 or 256");
+    GB_CHECK_ARG(t.fwd_items >= 1 && t.fwd_items <= 2 && t.b1_items >= 1 && t.b1_items <= 2,
+                 "items per SM must be 1 or 2");
+    const int zf = choose_zt(K, p->N, p->nz, true, t.fwd_tpb);
+    const int zb = choose_zt(K, p->N, p->nz, false);
+    if (!zf || !zb) {
+        set_error("the %d-thread forward tile does not fit shared memory", t.fwd_tpb);
+        return GB_ERR_UNSUPPORTED;
+    }
+    if (t.fwd_zt == 0) t.fwd_zt = zf;
+    if (t.b1_zt == 0) t.b1_zt = zb;
+    GB_CHECK_ARG(t.fwd_zt > 0 && t.fwd_zt <= zf && (t.fwd_zt % OB == 0 || t.fwd_zt == p->nz),
+                 "fwd_zt must be a multiple of %d in (0, %d]", OB, zf);
+    GB_CHECK_ARG(t.b1_zt > 0 && t.b1_zt <= zb && (t.b1_zt % OB == 0 || t.b1_zt == p->nz),
+                 "b1_zt must be a multiple of %d in (0, %d]", OB, zb);
+    return GB_OK;
+}
+
+gb_status gb_spect_set_tuning(gb_spect_plan *p, const gb_spect_tuning *tuning) {
+    clear_error();
+    GB_CHECK_ARG(p && tuning, "null argument");
+    if (!p->dev.psf) return GB_OK;  // the plain kernels have no tiles
+    gb_spect_tuning t = *tuning;
+    gb_status st = resolve_tuning(p, t);
+    if (st != GB_OK) return st;
+    const int K = p->dev.K;
+    GB_CUDA(setup_fwd(K, fwd_psf_smem_bytes(K, p->N, t.fwd_zt, t.fwd_tpb), t.fwd_tpb));
+    GB_CUDA(setup_b1(K, b1_psf_smem_bytes(K, p->N, t.b1_zt)));
+    p->fwd_tpb = t.fwd_tpb;
+    p->Zt_fwd = t.fwd_zt;
+    p->fwd_items = t.fwd_items;
+    p->Zt_b1 = t.b1_zt;
+    p->b1_items = t.b1_items;
+    return upload_lists(p, std::max(1, p->n_subsets));
+}
+
 static gb_status run_forward(gb_spect_plan *p, const float *obj, int subset, float *out,
                              int ratio, const float *gproj, const float *sadd, float *pred,
                              cudaStream_t st) {
@@ -577,7 +640,7 @@ static gb_status run_forward(gb_spect_plan *p, const float *obj, int subset, flo
     const gb_spect_plan::List &L = p->lists[li];
     const int *alist = p->d_alist + L.alist_off;
     GB_CUDA(launch_fwd(p->dev, obj, alist, p->d_items + L.fitem_off, L.n_fitems, p->Zt_fwd,
-                       p->d_partials, st));
+                       p->fwd_tpb, p->d_partials, st));
     GB_CUDA(launch_reduce(L.n, p->d_ioff + L.ioff_off, p->N * p->nz, p->d_partials, out, ratio,
                           gproj, sadd, alist, pred, st));
     return GB_OK;
@@ -633,6 +696,128 @@ gb_status gb_spect_backward(gb_spect_plan *p, const float *proj, float *obj, int
     }
     UpdateArgs u{};
     return run_backward(p, proj, li, adjoint ? 1 : 0, obj, B2_WRITE, u, as_stream(stream));
+}
+
+// Autotuner: time each candidate tile configuration of the forward kernel, then of the
+// back-projection kernel, on a temporary object of ones and keep the fastest.  The
+// candidates are the CTA size (512 threads, or 256 threads with two CTAs per SM when its
+// tile fits), the widest z slab and half of it, and one or two work items per CTA slot.
+gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
+                            gb_spect_tuning *out, gb_stream_t stream) {
+    clear_error();
+    GB_CHECK_ARG(p, "null plan");
+    GB_CHECK_ARG(reps >= 1 && reps <= 1000, "reps must be in [1, 1000]");
+    const int li = list_index(p, subset);
+    if (li < 0) {
+        set_error("subset %d out of range (n_subsets=%d)", subset, p->n_subsets);
+        return GB_ERR_STATE;
+    }
+    if (!p->dev.psf) return out ? gb_spect_get_tuning(p, out) : GB_OK;
+    cudaStream_t st = as_stream(stream);
+    const int K = p->dev.K, OB = (K <= 31) ? 8 : 4;
+    const size_t vol = (size_t)p->N * p->N * p->nz;
+    const size_t npr = (size_t)p->lists[li].n * p->N * p->nz;
+    float *obj = nullptr, *proj = nullptr, *back = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    gb_status rc = GB_OK;
+    gb_spect_tuning best{};
+    gb_spect_get_tuning(p, &best);
+    auto cleanup = [&]() {
+        cudaFree(obj);
+        cudaFree(proj);
+        cudaFree(back);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+#define TUNE_CUDA(call)                                                                \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            set_error("%s failed: %s", #call, cudaGetErrorString(e_));                 \
+            cleanup();                                                                 \
+            return e_ == cudaErrorMemoryAllocation ? GB_ERR_OOM : GB_ERR_CUDA;         \
+        }                                                                              \
+    } while (0)
+    TUNE_CUDA(cudaMalloc(&obj, vol * sizeof(float)));
+    TUNE_CUDA(cudaMalloc(&proj, npr * sizeof(float)));
+    TUNE_CUDA(cudaMalloc(&back, vol * sizeof(float)));
+    {
+        std::vector<float> ones(vol, 1.0f);
+        TUNE_CUDA(cudaMemcpy(obj, ones.data(), vol * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    TUNE_CUDA(cudaEventCreate(&e0));
+    TUNE_CUDA(cudaEventCreate(&e1));
+    // mean time of one call over `reps` after one untimed call; < 0 on failure
+    auto time_ms = [&](auto &&call) -> float {
+        if (call() != GB_OK) return -1.f;
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < reps; r++)
+            if (call() != GB_OK) return -1.f;
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms / reps;
+    };
+    auto fwd_call = [&]() {
+        return run_forward(p, obj, subset, proj, 0, nullptr, nullptr, nullptr, st);
+    };
+    auto bwd_call = [&]() { return run_backward(p, proj, li, 0, back, B2_WRITE, UpdateArgs{}, st); };
+    // forward candidates
+    float best_ms = 1e30f;
+    gb_spect_tuning fbest = best;
+    for (int tpb : {512, 256}) {
+        const int zmax = choose_zt(K, p->N, p->nz, true, tpb);
+        if (!zmax) continue;
+        for (int zt : {zmax, (zmax / 2) / OB * OB}) {
+            if (zt < 2 * OB || (zt != zmax && zt >= p->nz)) continue;
+            for (int items : {1, 2}) {
+                gb_spect_tuning t = best;
+                t.fwd_tpb = tpb;
+                t.fwd_zt = zt;
+                t.fwd_items = items;
+                if (gb_spect_set_tuning(p, &t) != GB_OK) continue;
+                const float ms = time_ms(fwd_call);
+                if (ms >= 0.f && ms < best_ms) {
+                    best_ms = ms;
+                    fbest = t;
+                }
+            }
+        }
+    }
+    best.fwd_tpb = fbest.fwd_tpb;
+    best.fwd_zt = fbest.fwd_zt;
+    best.fwd_items = fbest.fwd_items;
+    // back-projection candidates (with the chosen forward tiles)
+    best_ms = 1e30f;
+    gb_spect_tuning bbest = best;
+    const int zbmax = choose_zt(K, p->N, p->nz, false);
+    for (int zt : {zbmax, (zbmax / 2) / OB * OB}) {
+        if (zt < 2 * OB || (zt != zbmax && zt >= p->nz)) continue;
+        for (int items : {1, 2}) {
+            gb_spect_tuning t = best;
+            t.b1_zt = zt;
+            t.b1_items = items;
+            if (gb_spect_set_tuning(p, &t) != GB_OK) continue;
+            const float ms = time_ms(bwd_call);
+            if (ms >= 0.f && ms < best_ms) {
+                best_ms = ms;
+                bbest = t;
+            }
+        }
+    }
+    best.b1_zt = bbest.b1_zt;
+    best.b1_items = bbest.b1_items;
+#undef TUNE_CUDA
+    cudaError_t le = cudaGetLastError();
+    cleanup();
+    if (le != cudaSuccess) {
+        set_error("autotune launch failed: %s", cudaGetErrorString(le));
+        return GB_ERR_CUDA;
+    }
+    rc = gb_spect_set_tuning(p, &best);
+    if (rc == GB_OK && out) *out = best;
+    return rc;
 }
 
 gb_status gb_spect_osem_step(gb_spect_plan *p, float *obj, const float *g, const float *s,
@@ -722,6 +907,7 @@ bool plan_forward_args(const gb_spect_plan *p, int subset, FwdArgs *a) {
     a->n_items = L.n_fitems;
     a->ioff = p->d_ioff + L.ioff_off;
     a->Zt = p->Zt_fwd;
+    a->tpb = p->fwd_tpb;
     return true;
 }
 

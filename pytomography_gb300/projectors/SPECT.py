@@ -30,16 +30,23 @@ class SPECTSystemMatrix(SystemMatrix):
         psf_trunc_rel: PSF taps below this fraction of a plane's largest tap are skipped
             (default 1e-7: changes projections by well under 1e-6 relative; 0 keeps every
             tap of the reference's kernel).
+        autotune: time the kernels' tile candidates on the device whenever the subsets
+            change (results are cached per geometry for the process) instead of using the
+            shared-memory-derived defaults.  Tiles change no result beyond the order of
+            floating-point sums.
     """
+
+    _tuning_cache: dict = {}
 
     def __init__(self, obj2obj_transforms, proj2proj_transforms, object_meta, proj_meta,
                  object_initial_based_on_camera_path: bool = False,
-                 psf_trunc_rel: float = 1e-7) -> None:
+                 psf_trunc_rel: float = 1e-7, autotune: bool = False) -> None:
         if proj2proj_transforms:
             raise NotImplementedError("proj2proj transforms are not part of the fused path")
         super().__init__(object_meta, proj_meta, obj2obj_transforms, proj2proj_transforms)
         self.object_initial_based_on_camera_path = object_initial_based_on_camera_path
         self.psf_trunc_rel = float(psf_trunc_rel)
+        self.autotune_enabled = bool(autotune)
         self._plan = None
         self._lib = _lib.load()
         self._build_plan()
@@ -155,6 +162,46 @@ class SPECTSystemMatrix(SystemMatrix):
         self.subset_indices_array = [indices[i::n_subsets] for i in range(n_subsets)]
         self.n_subsets = n_subsets
         _lib.check(self._lib.gb_spect_set_subsets(self._plan, int(n_subsets)))
+        if self.autotune_enabled:
+            self.autotune()
+
+    # ------------------------------------------------------------ tiles
+    def _tuning_key(self, subset_idx):
+        props = torch.cuda.get_device_properties(self.device)
+        return (props.name, tuple(int(v) for v in self.object_meta.shape),
+                tuple(float(v) for v in self.object_meta.dr), self._order, self._psf_k,
+                int(self.proj_meta.num_projections), int(self.n_subsets),
+                self._n_sel(subset_idx))
+
+    def get_tuning(self) -> dict:
+        t = _lib.SpectTuning()
+        _lib.check(self._lib.gb_spect_get_tuning(self._plan, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **fields) -> None:
+        t = _lib.SpectTuning(**{**self.get_tuning(), **fields})
+        _lib.check(self._lib.gb_spect_set_tuning(self._plan, ctypes.byref(t)))
+
+    def autotune(self, subset_idx: int | None = 0, reps: int = 3) -> dict:
+        """Pick the fastest kernel tiles for this geometry (gb_spect_autotune), timing
+        the projections of ``subset_idx`` (the first subset by default, all angles when
+        there are no subsets); repeated geometries reuse the first result."""
+        if self.n_subsets <= 1:
+            subset_idx = None
+        key = self._tuning_key(subset_idx)
+        hit = SPECTSystemMatrix._tuning_cache.get(key)
+        if hit is not None:
+            self.set_tuning(**hit)
+            return dict(hit)
+        out = _lib.SpectTuning()
+        with torch.cuda.device(self.device):
+            torch.cuda.synchronize()
+            _lib.check(self._lib.gb_spect_autotune(
+                self._plan, self._subset_code(subset_idx), int(reps), ctypes.byref(out),
+                _lib.stream_handle(self.device)))
+            torch.cuda.synchronize()
+        SPECTSystemMatrix._tuning_cache[key] = out.as_dict()
+        return out.as_dict()
 
     def get_projection_subset(self, projections: torch.Tensor, subset_idx: int) -> torch.Tensor:
         return projections[..., self.subset_indices_array[subset_idx], :, :]
