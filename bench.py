@@ -383,8 +383,8 @@ def main():
     ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
     ap.add_argument("--profile-case", action="store_true",
                     help="run 3 fused sub-iterations of the workload and exit (for ncu)")
-    ap.add_argument("--workload", default="osem128",
-                    choices=["osem128", "serving", "pet", "autograd"],
+    ap.add_argument("--workload", default="osem128",  # osem64: the 64^3 / 64-angle att case
+                    choices=["osem128", "osem64", "serving", "pet", "autograd"],
                     help="osem128: the 128^3 x 120-angle reconstruction (default); serving: "
                          "32 uneven reconstructions, batched vs plain; pet: TOF listmode OSEM "
                          "(10M events); autograd: Poisson-NLL gradients of 8 objects + BSREM")
@@ -418,7 +418,8 @@ def main():
     if args.workload == "autograd":
         return run_autograd(args, dev)
 
-    w = synthetic.config2()
+    w = synthetic.config1() if args.workload == "osem64" else synthetic.config2()
+    metric = METRIC if args.workload != "osem64" else "OSEM subiter/s at 64^3x64 ang (att)"
     H = synthetic.build_system_matrix(w)
     g_host = synthetic.poisson_projections(H, w)
     g = g_host.to(dev)
@@ -427,6 +428,7 @@ def main():
     nbps = [nb.contiguous() for nb in lik.norm_BPs]
     f = torch.ones(w.shape, device=dev)
     n_sub = w.n_subsets
+    n_sel = len(w.angles) // n_sub  # angles per sub-iteration (equal subsets here)
     if args.profile_case:
         for k in range(3):
             H.osem_step(f, g, None, nbps[k], k)
@@ -472,7 +474,7 @@ def main():
 
     # ---- fused sub-iterations, one CUDA graph per subset
     f.fill_(1.0)
-    pred = torch.empty((12, *w.shape[1:]), device=dev)
+    pred = torch.empty((n_sel, *w.shape[1:]), device=dev)
     stream = torch.cuda.Stream(device=dev)
     graphs = []
     with torch.cuda.stream(stream):
@@ -510,8 +512,8 @@ def main():
     value = world * args.steps / (ms / 1000.0)
 
     # ---- roofline of the forward projector (kernels launched on `cur`)
-    fwd_bytes, bwd_bytes, sub_bytes = alg_bytes_subiter()
-    proj = torch.empty((12, *w.shape[1:]), device=dev)
+    fwd_bytes, bwd_bytes, sub_bytes = alg_bytes_subiter(w.shape[0], n_sel, 1)
+    proj = torch.empty((n_sel, *w.shape[1:]), device=dev)
     obj = torch.empty(w.shape, device=dev)
     for _ in range(3):
         lib = H._lib
@@ -556,23 +558,42 @@ def main():
     e2e_subiter = w.n_iters * w.n_subsets / float(np.mean(e2e_times))
 
     cpu = None
+    cpu_torch = None
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
         c = CpuSubiter(w, cores)
         t = c.angles(c.idx)
         cpu = {"value": 1.0 / t, "unit": "subiter/s", "cores": cores, "kind": "port",
-               "sample": "one OSEM sub-iteration (12 angles fwd+ratio+bwd+update) of the "
-                         "128^3 workload, float32 C/OpenMP oracle"}
+               "sample": f"one OSEM sub-iteration ({n_sel} angles fwd+ratio+bwd+update) of "
+                         f"the {w.shape[0]}^3 workload, float32 C/OpenMP oracle"}
+        # the reference's per-call PyTorch sequence on the host cores: two angles of the
+        # first subset forward + back projected, scaled to the 12-angle sub-iteration
+        torch.set_num_threads(cores)
+        Rc = TorchReferenceProjector(H, device="cpu")
+        two = [int(i) for i in H.subset_indices_array[0][:2].tolist()]
+        fc = torch.ones(w.shape)
+        Rc.forward(fc, two[:1])
+        t0 = time.perf_counter()
+        pc = Rc.forward(fc, two)
+        Rc.backward(torch.ones_like(pc), two)
+        t_two = time.perf_counter() - t0
+        cpu_torch = {"value": 2.0 / (t_two * n_sel), "unit": "subiter/s", "cores": cores,
+                     "kind": "port", "sample": "the reference's per-call PyTorch sequence "
+                     "(tests/torch_reference.py) on torch CPU with all host threads: 2 "
+                     f"angles forward + back projected, scaled to {n_sel}"}
+        del Rc
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "subiter/s", "n_gpus": world,
+            "metric": metric, "value": value, "unit": "subiter/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": fused_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": w.name, "subsets": n_sub, "angles_per_step": 12,
+            "config": {"workload": w.name, "subsets": n_sub, "angles_per_step": n_sel,
                        "l2": "no flush; per-step working set (A 175 MB + W 175 MB + object) "
-                             "exceeds the 129 MB L2",
+                             "exceeds the 129 MB L2" if w.shape[0] == 128 else
+                             "no flush; per-step working set (A + W + object, ~60 MB) is "
+                             "smaller than L2: the figure includes L2 reuse across steps",
                        "parallelism": "replicas" if world > 1 else "single"},
             "plain": {"value": 1000.0 / plain_ms, "unit": "subiter/s", "ms_per_step": plain_ms},
             "fused_vs_plain": plain_ms / fused_ms,
@@ -586,9 +607,11 @@ def main():
                                               / (w.n_iters * w.n_subsets)),
                     "d2h_bytes_per_step": int(out_host.numel() * 4 / (w.n_iters * w.n_subsets)),
                     "what": "OSEM(4,10) from host tensors incl. plan build and normalisation"},
-            "roofline": {"bound": "hbm", "kernel": "forward projector (k_fwd_psf + k_reduce)",
+            "roofline": {"bound": "hbm", "kernel": "forward projector (k_fwd_psf + k_reduce)"
+                         if w.psf else "forward projector (k_fwd_nopsf + k_reduce)",
                          "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                         "peak_kind": peak_kind, "traffic": FWD_DRAM_BYTES_PER_LAUNCH,
+                         "peak_kind": peak_kind,
+                         "traffic": FWD_DRAM_BYTES_PER_LAUNCH if w.shape[0] == 128 else None,
                          "traffic_source": "ncu dram__bytes_read+write, one launch",
                          "alg_bytes_per_launch": fwd_bytes, "launch_ms": fwd_ms},
             "backward_ms": bwd_ms,
@@ -596,6 +619,7 @@ def main():
             "gpu_launches": 4 * args.steps,
             "clocks": clocks.summary() if clocks else None,
             "cpu_baseline": cpu,
+            "cpu_torch_reference": cpu_torch,
         }
         print(json.dumps(line))
     if dist:

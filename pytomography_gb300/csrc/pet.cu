@@ -22,6 +22,8 @@
 #include <cmath>
 #include <vector>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "common.cuh"
 
 namespace gb {
@@ -134,44 +136,96 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
     return acc;
 }
 
-// Listmode events of a subset: event e = first + j * stride, j < n.
-// mode 0: out[j] = H img;  mode 1 (ratio): out[j] = 1 / (H img + s[e] + delta)
+// Event tiles: the events of a list (every event, or one subset i::n) sorted by a
+// locality key, packed as {id1, id2, centred TOF bin, j} where j is the event's position
+// in the list (event index first + j * stride).  Threads of a warp then trace nearby,
+// nearly parallel LORs: their image reads share L1 lines and their back-projection
+// atomics share L2 sectors.  Outputs indexed by j keep the list order.
+//
+// mode 0: out[k or j] = H img;  mode 1 (ratio): out[k] = num[e] / (H img + s[e] + delta)
 template <bool TOF>
 __global__ void __launch_bounds__(256)
-    k_pet_fwd(PetDev g, const int *__restrict__ ev, int ncol, long long first, long long stride,
+    k_pet_fwd(PetDev g, const int4 *__restrict__ rec, long long first, long long stride,
               long long n, const float *__restrict__ img, float *__restrict__ out, int ratio,
               const float *__restrict__ sadd, const float *__restrict__ gnum, int gnum_len) {
-    long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    long long e = first + j * stride;
-    const int *r = ev + e * ncol;
-    const float *p0 = g.lut + 3 * (long long)r[0];
-    const float *p1 = g.lut + 3 * (long long)r[1];
-    int tb = TOF ? r[2] - g.bin_shift : 0;
-    float v = joseph<false, TOF>(g, p0, p1, nullptr, img, tb, 0.f);
-    if (ratio) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int4 r = rec[k];
+    const float *p0 = g.lut + 3 * (long long)r.x;
+    const float *p1 = g.lut + 3 * (long long)r.y;
+    float v = joseph<false, TOF>(g, p0, p1, nullptr, img, r.z, 0.f);
+    if (ratio) {  // internal ratio array, tile order
+        const long long e = first + (long long)r.w * stride;
         float pr = sadd ? v + sadd[e] : v;
         float num = gnum_len > 1 ? gnum[e] : gnum[0];
-        out[j] = num / (pr + 1e-11f);
+        out[k] = num / (pr + 1e-11f);
     } else {
-        out[j] = v;
+        out[r.w] = v;
     }
 }
 
+// proj in tile order (sorted = 1, the fused step's ratio array) or list order (0)
 template <bool TOF>
 __global__ void __launch_bounds__(256)
-    k_pet_bwd(PetDev g, const int *__restrict__ ev, int ncol, long long first, long long stride,
-              long long n, const float *__restrict__ proj, float *__restrict__ img) {
+    k_pet_bwd(PetDev g, const int4 *__restrict__ rec, long long n,
+              const float *__restrict__ proj, int sorted, float *__restrict__ img) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int4 r = rec[k];
+    const float v = proj[sorted ? k : (long long)r.w];
+    if (v == 0.f) return;
+    const float *p0 = g.lut + 3 * (long long)r.x;
+    const float *p1 = g.lut + 3 * (long long)r.y;
+    joseph<true, TOF>(g, p0, p1, img, nullptr, r.z, v);
+}
+
+// Locality key of list event j: principal axis (2 bits), transaxial direction in 8 bins
+// over [0, pi) (3 bits) and the Morton code of the TOF-window centre (the LOR midpoint
+// without TOF) in cells of 8 voxels, 6 bits per axis (18 bits).
+__device__ __forceinline__ unsigned morton3(unsigned x, unsigned y, unsigned z) {
+    unsigned m = 0;
+#pragma unroll
+    for (int b = 0; b < 6; b++)
+        m |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) |
+             (((z >> b) & 1u) << (3 * b + 2));
+    return m;
+}
+
+__global__ void k_pet_keys(PetDev g, const int *__restrict__ ev, int ncol, long long first,
+                           long long stride, long long n, unsigned *__restrict__ keys,
+                           int *__restrict__ vals) {
     long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    long long e = first + j * stride;
-    const int *r = ev + e * ncol;
-    const float v = proj[j];
-    if (v == 0.f) return;
+    const int *r = ev + (first + j * stride) * ncol;
     const float *p0 = g.lut + 3 * (long long)r[0];
     const float *p1 = g.lut + 3 * (long long)r[1];
-    int tb = TOF ? r[2] - g.bin_shift : 0;
-    joseph<true, TOF>(g, p0, p1, img, nullptr, tb, v);
+    const float d[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    const float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const float ad0 = fabsf(d[0]), ad1 = fabsf(d[1]), ad2 = fabsf(d[2]);
+    const unsigned axis = ad2 > fmaxf(ad0, ad1) ? 2u : (ad1 > ad0 ? 1u : 0u);
+    float phi = atan2f(d[1], d[0]);
+    if (phi < 0.f) phi += 3.14159265f;
+    const unsigned dir = min(7u, (unsigned)(phi * (8.f / 3.14159265f)));
+    const float tc = (g.tof && len > 0.f) ? ((r[2] - g.bin_shift) * g.bw + g.co) / len : 0.f;
+    unsigned cell[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float c = 0.5f * (p0[a] + p1[a]) + tc * d[a];
+        const float u = (c - (g.org[a] - 0.5f * g.vox[a])) / (8.f * g.vox[a]);
+        cell[a] = (unsigned)min(63, max(0, (int)floorf(u)));
+    }
+    keys[j] = ((axis * 8u + dir) << 18) | morton3(cell[0], cell[1], cell[2]);
+    vals[j] = (int)j;
+}
+
+__global__ void k_pet_pack(const int *__restrict__ ev, int ncol, int bin_shift, int tof,
+                           long long first, long long stride, long long n,
+                           const int *__restrict__ order, int4 *__restrict__ rec) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int j = order[k];
+    const int *r = ev + (first + (long long)j * stride) * ncol;
+    rec[k] = make_int4(r[0], r[1], tof ? r[2] - bin_shift : 0, j);
 }
 
 // Sensitivity: non-TOF back projection of (w * exp(-H mu) + delta) over a LOR set given
@@ -235,6 +289,9 @@ struct gb_pet_plan {
     int n_subsets = 1;
     float *d_ratio = nullptr, *d_bp = nullptr;
     long long img_size = 0;
+    // event tiles: list 0 = every event, list s + 1 = subset s (i::n_subsets)
+    int4 *d_rec = nullptr;
+    std::vector<long long> list_off;
 };
 
 static void pet_free(gb_pet_plan *p) {
@@ -243,6 +300,7 @@ static void pet_free(gb_pet_plan *p) {
     cudaFree(p->d_ev);
     cudaFree(p->d_ratio);
     cudaFree(p->d_bp);
+    cudaFree(p->d_rec);
     delete p;
 }
 
@@ -257,6 +315,69 @@ static void subset_range(const gb_pet_plan *p, int subset, long long &first, lon
         stride = p->n_subsets;
         n = p->n_events > subset ? (p->n_events - subset + p->n_subsets - 1) / p->n_subsets : 0;
     }
+}
+
+// Sort the events of every list by their locality key (device radix sort, stable, so
+// equal keys keep list order) and pack the tiles.
+static gb_status build_tiles(gb_pet_plan *p, int n_subsets) {
+    const long long E = p->n_events;
+    cudaFree(p->d_rec);
+    p->d_rec = nullptr;
+    p->list_off.assign(1, 0);
+    if (E == 0) {
+        for (int s = 0; s < n_subsets; s++) p->list_off.push_back(0);
+        return GB_OK;
+    }
+    GB_CUDA(cudaMalloc(&p->d_rec, (size_t)(2 * E) * sizeof(int4)));
+    unsigned *keys = nullptr, *keys2 = nullptr;
+    int *vals = nullptr, *vals2 = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    cudaError_t e = cudaSuccess;
+    auto fail = [&](cudaError_t err) {
+        cudaFree(keys); cudaFree(keys2); cudaFree(vals); cudaFree(vals2); cudaFree(tmp);
+        set_error("event tile build failed: %s", cudaGetErrorString(err));
+        return err == cudaErrorMemoryAllocation ? GB_ERR_OOM : GB_ERR_CUDA;
+    };
+    if ((e = cudaMalloc(&keys, E * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMalloc(&keys2, E * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMalloc(&vals, E * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc(&vals2, E * sizeof(int))) != cudaSuccess)
+        return fail(e);
+    if ((e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2,
+                                             (int)E, 0, 23)) != cudaSuccess ||
+        (e = cudaMalloc(&tmp, tmp_bytes)) != cudaSuccess)
+        return fail(e);
+    long long off = 0;
+    for (int li = 0; li <= n_subsets; li++) {
+        long long first = 0, stride = 1, n = E;
+        if (li > 0) {
+            first = li - 1;
+            stride = n_subsets;
+            n = E > first ? (E - first + stride - 1) / stride : 0;
+        }
+        if (li > 0) p->list_off.push_back(off);
+        if (n == 0) continue;
+        const unsigned blocks = (unsigned)((n + 255) / 256);
+        k_pet_keys<<<blocks, 256>>>(p->dev, p->d_ev, p->ncol, first, stride, n, keys, vals);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+        size_t tb = tmp_bytes;
+        if ((e = cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, vals2, (int)n, 0,
+                                                 23)) != cudaSuccess)
+            return fail(e);
+        k_pet_pack<<<blocks, 256>>>(p->d_ev, p->ncol, p->dev.bin_shift, p->dev.tof, first, stride,
+                                    n, vals2, p->d_rec + off);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+        off += n;
+    }
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
+    cudaFree(keys); cudaFree(keys2); cudaFree(vals); cudaFree(vals2); cudaFree(tmp);
+    return GB_OK;
+}
+
+// The tiles of a subset (-1 = every event).
+static const int4 *list_tiles(const gb_pet_plan *p, int subset) {
+    return p->d_rec ? p->d_rec + (subset < 0 ? 0 : p->list_off[subset + 1]) : nullptr;
 }
 
 extern "C" {
@@ -317,6 +438,11 @@ gb_status gb_pet_plan_create(const gb_pet_desc *d, gb_pet_plan **out) {
                 }
             }
     }
+    gb_status st = build_tiles(p, 1);
+    if (st != GB_OK) {
+        pet_free(p);
+        return st;
+    }
     *out = p;
     return GB_OK;
 }
@@ -333,6 +459,8 @@ gb_status gb_pet_plan_destroy(gb_pet_plan *p) {
 gb_status gb_pet_set_subsets(gb_pet_plan *p, int32_t n_subsets) {
     clear_error();
     GB_CHECK_ARG(p && n_subsets >= 1, "invalid subsets");
+    gb_status st = build_tiles(p, n_subsets);
+    if (st != GB_OK) return st;
     p->n_subsets = n_subsets;
     return GB_OK;
 }
@@ -346,14 +474,13 @@ gb_status gb_pet_forward(gb_pet_plan *p, const float *img, float *proj, int32_t 
     subset_range(p, subset, first, stride, n);
     if (n == 0) return GB_OK;
     unsigned blocks = (unsigned)((n + 255) / 256);
+    const int4 *rec = list_tiles(p, subset);
     if (p->dev.tof)
-        k_pet_fwd<true><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, p->d_ev, p->ncol, first,
-                                                               stride, n, img, proj, 0, nullptr,
-                                                               nullptr, 0);
+        k_pet_fwd<true><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, rec, first, stride, n, img,
+                                                               proj, 0, nullptr, nullptr, 0);
     else
-        k_pet_fwd<false><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, p->d_ev, p->ncol, first,
-                                                                stride, n, img, proj, 0, nullptr,
-                                                                nullptr, 0);
+        k_pet_fwd<false><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, rec, first, stride, n,
+                                                                img, proj, 0, nullptr, nullptr, 0);
     GB_LAUNCH_CHECK();
     return GB_OK;
 }
@@ -369,12 +496,11 @@ gb_status gb_pet_backward(gb_pet_plan *p, const float *proj, float *img, int32_t
     GB_CUDA(cudaMemsetAsync(img, 0, (size_t)p->img_size * sizeof(float), st));
     if (n == 0) return GB_OK;
     unsigned blocks = (unsigned)((n + 255) / 256);
+    const int4 *rec = list_tiles(p, subset);
     if (p->dev.tof)
-        k_pet_bwd<true><<<blocks, 256, 0, st>>>(p->dev, p->d_ev, p->ncol, first, stride, n, proj,
-                                                img);
+        k_pet_bwd<true><<<blocks, 256, 0, st>>>(p->dev, rec, n, proj, 0, img);
     else
-        k_pet_bwd<false><<<blocks, 256, 0, st>>>(p->dev, p->d_ev, p->ncol, first, stride, n, proj,
-                                                 img);
+        k_pet_bwd<false><<<blocks, 256, 0, st>>>(p->dev, rec, n, proj, 0, img);
     GB_LAUNCH_CHECK();
     return GB_OK;
 }
@@ -391,25 +517,24 @@ gb_status gb_pet_osem_step(gb_pet_plan *p, float *img, const float *numerator,
     subset_range(p, subset, first, stride, n);
     cudaStream_t st = as_stream(stream);
     unsigned blocks = (unsigned)((n + 255) / 256);
+    const int4 *rec = list_tiles(p, subset);
     if (n > 0) {
         if (p->dev.tof)
-            k_pet_fwd<true><<<blocks, 256, 0, st>>>(p->dev, p->d_ev, p->ncol, first, stride, n,
-                                                    img, p->d_ratio, 1, additive, numerator,
+            k_pet_fwd<true><<<blocks, 256, 0, st>>>(p->dev, rec, first, stride, n, img,
+                                                    p->d_ratio, 1, additive, numerator,
                                                     (int)numerator_len);
         else
-            k_pet_fwd<false><<<blocks, 256, 0, st>>>(p->dev, p->d_ev, p->ncol, first, stride, n,
-                                                     img, p->d_ratio, 1, additive, numerator,
+            k_pet_fwd<false><<<blocks, 256, 0, st>>>(p->dev, rec, first, stride, n, img,
+                                                     p->d_ratio, 1, additive, numerator,
                                                      (int)numerator_len);
         GB_LAUNCH_CHECK();
     }
     GB_CUDA(cudaMemsetAsync(p->d_bp, 0, (size_t)p->img_size * sizeof(float), st));
     if (n > 0) {
         if (p->dev.tof)
-            k_pet_bwd<true><<<blocks, 256, 0, st>>>(p->dev, p->d_ev, p->ncol, first, stride, n,
-                                                    p->d_ratio, p->d_bp);
+            k_pet_bwd<true><<<blocks, 256, 0, st>>>(p->dev, rec, n, p->d_ratio, 1, p->d_bp);
         else
-            k_pet_bwd<false><<<blocks, 256, 0, st>>>(p->dev, p->d_ev, p->ncol, first, stride, n,
-                                                     p->d_ratio, p->d_bp);
+            k_pet_bwd<false><<<blocks, 256, 0, st>>>(p->dev, rec, n, p->d_ratio, 1, p->d_bp);
         GB_LAUNCH_CHECK();
     }
     k_pet_update<<<(unsigned)((p->img_size + 255) / 256), 256, 0, st>>>(img, p->d_bp, norm_bp,
@@ -442,18 +567,18 @@ gb_status gb_pet_lor_forward(gb_pet_plan *p, const float *img, float *proj, int3
                              int32_t use_tof, gb_stream_t stream) {
     clear_error();
     GB_CHECK_ARG(p && img && proj, "null argument");
+    GB_CHECK_ARG(subset < p->n_subsets, "subset out of range");
     long long first, stride, n;
     subset_range(p, subset, first, stride, n);
     if (n == 0) return GB_OK;
     unsigned blocks = (unsigned)((n + 255) / 256);
+    const int4 *rec = list_tiles(p, subset);
     if (use_tof && p->dev.tof)
-        k_pet_fwd<true><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, p->d_ev, p->ncol, first,
-                                                               stride, n, img, proj, 0, nullptr,
-                                                               nullptr, 0);
+        k_pet_fwd<true><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, rec, first, stride, n, img,
+                                                               proj, 0, nullptr, nullptr, 0);
     else
-        k_pet_fwd<false><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, p->d_ev, p->ncol, first,
-                                                                stride, n, img, proj, 0, nullptr,
-                                                                nullptr, 0);
+        k_pet_fwd<false><<<blocks, 256, 0, as_stream(stream)>>>(p->dev, rec, first, stride, n,
+                                                                img, proj, 0, nullptr, nullptr, 0);
     GB_LAUNCH_CHECK();
     return GB_OK;
 }

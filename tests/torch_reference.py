@@ -28,11 +28,11 @@ import torch.nn.functional as F
 
 
 class TorchReferenceProjector:
-    def __init__(self, H) -> None:
+    def __init__(self, H, device=None) -> None:
         from pytomography_gb300.transforms.SPECT import SPECTAttenuationTransform, \
             SPECTPSFTransform
         self.H = H
-        self.device = H.device
+        self.device = H.device if device is None else torch.device(device)
         self.N = int(H.object_meta.shape[0])
         self.nz = int(H.object_meta.shape[2])
         self.pad = int(H.object_meta.pad_size)
@@ -85,6 +85,8 @@ class TorchReferenceProjector:
     def _angles(self, subset_idx):
         if subset_idx is None:
             return list(range(self.H.proj_meta.num_projections))
+        if isinstance(subset_idx, (list, tuple)):  # explicit angle indices
+            return [int(i) for i in subset_idx]
         return [int(i) for i in self.H.subset_indices_array[subset_idx].tolist()]
 
     # ------------------------------------------------------------------ operators
