@@ -203,6 +203,12 @@ def run_pet(args, dev):
     f = H._get_object_initial().contiguous()
     nbps = [lik._get_normBP(k).contiguous() for k in range(w.n_subsets)]
     k_state = [0]
+    if args.profile_case:
+        for k in range(3):
+            H.osem_step(f, lik.projections, s, nbps[k], k)
+        torch.cuda.synchronize()
+        print("profile case done")
+        return
 
     def fused():
         k = k_state[0] % w.n_subsets

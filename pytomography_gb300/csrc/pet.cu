@@ -28,6 +28,12 @@
 
 namespace gb {
 
+// TOF bin weight table: w(x) = (erfc((x - bw/2) q) - erfc((x + bw/2) q)) / 2 at
+// x = m * lim / kTofTab, m = 0 .. kTofTab (+1 guard), q = 1 / (sqrt(2) sigma), computed
+// in double on the host; linear interpolation in |s| (error below 1e-7 of the peak
+// weight at the benchmark's sigma, bin width and n_sigmas).
+constexpr int kTofTab = 4096;
+
 struct PetDev {
     int n[3];
     float vox[3], org[3];
@@ -36,6 +42,8 @@ struct PetDev {
     int tof;
     float bw, sig, co, nsig;
     int bin_shift;
+    const float *tof_tab;  // [kTofTab + 2]
+    float tof_inv_step;    // kTofTab / lim
 };
 
 __device__ __forceinline__ float pick(float a, float b, float c, int k) {
@@ -46,8 +54,12 @@ __device__ __forceinline__ int pick(int a, int b, int c, int k) {
 }
 
 // Joseph trace of one LOR.  BACK = false: returns sum of weighted samples of cimg.
-// BACK = true: adds val * weights into img (atomics).  Axis-dependent quantities are
-// selected into registers once (no dynamically indexed local arrays).
+// BACK = true: adds val * weights into img (atomics; the two corners of a bilinear pair
+// that are neighbours in z go out as one 8-byte vector atomic when aligned).
+// Along the principal axis k the plane parameter t, the sample coordinates on the two
+// other axes (in voxel units) and the TOF distance s are linear in the plane index i and
+// are evaluated as base + i * step.  Axis-dependent quantities are selected into
+// registers once (no dynamically indexed local arrays).
 template <bool BACK, bool TOF>
 __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict__ p0,
                                         const float *__restrict__ p1, float *img,
@@ -66,7 +78,7 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
         if (ez > (k == 0 ? ex : ey)) k = 2;
     }
     const int a = (k + 1) % 3, b = (k + 2) % 3;
-    const int strides[3] = {g.n[1] * g.n[2], g.n[2], 1};
+    const int nyz = g.n[1] * g.n[2];
     const float dk = pick(dx, dy, dz, k), da = pick(dx, dy, dz, a), db = pick(dx, dy, dz, b);
     const float pk = pick(ax, ay, az, k), pa0 = pick(ax, ay, az, a), pb0 = pick(ax, ay, az, b);
     const float vk = pick(g.vox[0], g.vox[1], g.vox[2], k);
@@ -78,9 +90,9 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
     const int nk = pick(g.n[0], g.n[1], g.n[2], k);
     const int na = pick(g.n[0], g.n[1], g.n[2], a);
     const int nb = pick(g.n[0], g.n[1], g.n[2], b);
-    const int sk = pick(strides[0], strides[1], strides[2], k);
-    const int sa = pick(strides[0], strides[1], strides[2], a);
-    const int sb = pick(strides[0], strides[1], strides[2], b);
+    const int sk = pick(nyz, g.n[2], 1, k);
+    const int sa = pick(nyz, g.n[2], 1, a);
+    const int sb = pick(nyz, g.n[2], 1, b);
     const float cf = vk * len / fabsf(dk);
     const float pk1 = pick(p1[0], p1[1], p1[2], k);
     const float lo = fminf(pk, pk1), hi = fmaxf(pk, pk1);
@@ -88,45 +100,70 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
     int i1 = (int)floorf((hi - ok) / vk);
     i0 = max(i0, 0);
     i1 = min(i1, nk - 1);
-    float tc = 0.f, lim = 0.f, isq = 0.f, hb = 0.f;
+    const float idk = 1.f / dk;
+    const float t0 = (ok - pk) * idk, dt = vk * idk;  // t(i) = t0 + i dt
+    const float iva = 1.f / va, ivb = 1.f / vb;
+    const float fa0 = (pa0 - oa + t0 * da) * iva, dfa = dt * da * iva;
+    const float fb0 = (pb0 - ob + t0 * db) * ivb, dfb = dt * db * ivb;
+    float s0 = 0.f, ds = 0.f, lim = 0.f;
     if (TOF) {
-        tc = tbin * g.bw + g.co;
+        const float tc = tbin * g.bw + g.co;
         lim = g.nsig * g.sig + g.bw / 2;
-        isq = 1.f / (sqrtf(2.f) * g.sig);
-        hb = g.bw / 2;
-        // planes with |s| <= lim: s(i) = ((o_k + i v_k - p0_k)/d_k - 1/2) len - tc;
-        // restrict [i0, i1] with one plane of slack, the exact test runs per plane
+        s0 = (t0 - 0.5f) * len - tc;  // s(i) = s0 + i ds: signed distance from the bin centre
+        ds = dt * len;
+        // planes with |s| <= lim, with one plane of slack; the exact test runs per plane
         float s_a = (((-lim + tc) / len + 0.5f) * dk + pk - ok) / vk;
         float s_b = (((lim + tc) / len + 0.5f) * dk + pk - ok) / vk;
         int ja = (int)floorf(fminf(s_a, s_b)) - 1, jb = (int)ceilf(fmaxf(s_a, s_b)) + 1;
         i0 = max(i0, ja);
         i1 = min(i1, jb);
     }
+    // the bilinear pair axis that is z (stride 1), if any: corners along it are neighbours
+    const bool zb = sb == 1, za = sa == 1;
     float acc = 0.f;
     for (int i = i0; i <= i1; i++) {
-        const float ck = ok + i * vk;
-        const float t = (ck - pk) / dk;
         float w = cf;
         if (TOF) {
-            const float s = (t - 0.5f) * len - tc;
-            if (fabsf(s) > lim) continue;
-            // (erf((s+h)q) - erf((s-h)q))/2 written with erfc of |s| (same value by
-            // symmetry) so the Gaussian tails do not cancel in float32
-            const float as = fabsf(s);
-            w *= 0.5f * (erfcf((as - hb) * isq) - erfcf((as + hb) * isq));
+            const float as = fabsf(fmaf((float)i, ds, s0));
+            if (as > lim) continue;
+            const float u = as * g.tof_inv_step;
+            const int m = min((int)u, kTofTab);
+            const float t0w = __ldg(g.tof_tab + m), t1w = __ldg(g.tof_tab + m + 1);
+            w *= fmaf(u - (float)m, t1w - t0w, t0w);
         }
-        const float pa = pa0 + t * da, pb = pb0 + t * db;
-        const float fa = (pa - oa) / va, fb = (pb - ob) / vb;
+        const float fa = fmaf((float)i, dfa, fa0), fb = fmaf((float)i, dfb, fb0);
         const float ga = floorf(fa), gb2 = floorf(fb);
         const int ia = (int)ga, ib = (int)gb2;
         const float wa = fa - ga, wb = fb - gb2;
-        const long long base = (long long)i * sk;
+        const int base = i * sk;
+        if (BACK && (zb || za)) {
+            // rows along the non-z axis, each with a z-neighbour pair
+            const int jz = zb ? ib : ia, jo = zb ? ia : ib;
+            const int nzz = zb ? nb : na, no = zb ? na : nb, so = zb ? sa : sb;
+            const float wz = zb ? wb : wa, wo = zb ? wa : wb;
+            const bool ok0 = (unsigned)jz < (unsigned)nzz, ok1 = (unsigned)(jz + 1) < (unsigned)nzz;
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int r = jo + q;
+                if ((unsigned)r >= (unsigned)no) continue;
+                const float wr = val * w * (q ? wo : 1.f - wo);
+                const float v0 = wr * (1.f - wz), v1 = wr * wz;
+                const int off = base + r * so + jz;
+                if (ok0 && ok1 && (off & 1) == 0) {
+                    atomicAdd(reinterpret_cast<float2 *>(img + off), make_float2(v0, v1));
+                } else {
+                    if (ok0) atomicAdd(img + off, v0);
+                    if (ok1) atomicAdd(img + off + 1, v1);
+                }
+            }
+            continue;
+        }
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int ja = ia + (q & 1), jb = ib + (q >> 1);
             if ((unsigned)ja >= (unsigned)na || (unsigned)jb >= (unsigned)nb) continue;
             const float wq = ((q & 1) ? wa : 1.f - wa) * ((q >> 1) ? wb : 1.f - wb);
-            const long long off = base + (long long)ja * sa + (long long)jb * sb;
+            const int off = base + ja * sa + jb * sb;
             if (BACK)
                 atomicAdd(img + off, val * w * wq);
             else
@@ -291,6 +328,7 @@ struct gb_pet_plan {
     long long img_size = 0;
     // event tiles: list 0 = every event, list s + 1 = subset s (i::n_subsets)
     int4 *d_rec = nullptr;
+    float *d_tof_tab = nullptr;
     std::vector<long long> list_off;
 };
 
@@ -301,6 +339,7 @@ static void pet_free(gb_pet_plan *p) {
     cudaFree(p->d_ratio);
     cudaFree(p->d_bp);
     cudaFree(p->d_rec);
+    cudaFree(p->d_tof_tab);
     delete p;
 }
 
@@ -415,6 +454,26 @@ gb_status gb_pet_plan_create(const gb_pet_desc *d, gb_pet_plan **out) {
         return GB_ERR_CUDA;
     }
     g.lut = p->d_lut;
+    if (d->tof) {
+        // TOF bin weight table over |s| in [0, n_sigmas sigma + bw/2]
+        const double h = 0.5 * d->tof_bin_width, q = 1.0 / (std::sqrt(2.0) * d->tof_sigma);
+        const double lim = (double)d->tof_n_sigmas * d->tof_sigma + h;
+        std::vector<float> tab(kTofTab + 2);
+        for (int m = 0; m <= kTofTab; m++) {
+            const double x = lim * m / kTofTab;
+            tab[m] = (float)(0.5 * (std::erfc((x - h) * q) - std::erfc((x + h) * q)));
+        }
+        tab[kTofTab + 1] = tab[kTofTab];
+        if ((e = cudaMalloc(&p->d_tof_tab, tab.size() * sizeof(float))) != cudaSuccess ||
+            (e = cudaMemcpy(p->d_tof_tab, tab.data(), tab.size() * sizeof(float),
+                            cudaMemcpyHostToDevice)) != cudaSuccess) {
+            set_error("TOF table upload failed: %s", cudaGetErrorString(e));
+            pet_free(p);
+            return GB_ERR_CUDA;
+        }
+        g.tof_tab = p->d_tof_tab;
+        g.tof_inv_step = (float)(kTofTab / lim);
+    }
     if (d->n_events > 0) {
         size_t bytes = (size_t)d->n_events * p->ncol * sizeof(int);
         if ((e = cudaMalloc(&p->d_ev, bytes)) != cudaSuccess ||

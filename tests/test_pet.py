@@ -35,7 +35,10 @@ def test_tof_meta_matches_reference():
 def test_scanner_lut_matches_reference():
     from pytomography_gb300.metadata.PET import get_scanner_LUT
     d = golden("pet_meta")
-    assert np.array_equal(get_scanner_LUT(INFO).numpy(), d["lut_small"])
+    # torch's float32 sin/cos may differ in the last bit between CPU architectures
+    # (the fixtures were made on x86-64): allow 2 ulp at the LUT's 120 mm scale
+    np.testing.assert_allclose(get_scanner_LUT(INFO).numpy(), d["lut_small"], rtol=0,
+                               atol=2 * np.spacing(np.float32(120.0)))
 
 
 def _events(lut, n, seed, nb=7, through=None):
