@@ -227,6 +227,59 @@ gb_status gb_pet_osem_step(gb_pet_plan *plan, float *img, const float *numerator
                            int64_t numerator_len, const float *additive, const float *norm_bp,
                            int32_t subset, gb_stream_t stream);
 
+/* ------------------------------------------------------------ PET sinogram
+ * Replaces the projection arithmetic of PETSinogramSystemMatrix
+ * (projectors/PET/pet_sinogram_system_matrix.py:12-296): the LOR of sinogram element
+ * (angle a, radial r, plane p) runs from (det_xy[a][r][0], plane_z[p][0]) to
+ * (det_xy[a][r][1], plane_z[p][1]) (_get_xyz_sinogram_coordinates, :50-85). */
+typedef struct gb_pet_sino_plan gb_pet_sino_plan;
+
+typedef struct gb_pet_sino_desc {
+    int32_t nx, ny, nz;        /* image shape [nx][ny][nz], z fastest */
+    float vx, vy, vz;          /* voxel size (mm) */
+    float ox, oy, oz;          /* centre of voxel (0,0,0) (mm) */
+    int32_t n_angles, n_radial, n_planes;  /* sinogram [n_angles][n_radial][n_planes] */
+    const float *det_xy;       /* host [n_angles][n_radial][2][2]: (x, y) of crystals 1, 2 */
+    const float *plane_z;      /* host [n_planes][2]: z of crystals 1, 2 */
+    int32_t tof;               /* 1: TOF sinograms (bin fastest) are available */
+    int32_t tof_num_bins;
+    float tof_bin_width;       /* mm */
+    float tof_sigma;           /* mm */
+    float tof_center_offset;   /* mm */
+    float tof_n_sigmas;
+} gb_pet_sino_desc;
+
+gb_status gb_pet_sino_plan_create(const gb_pet_sino_desc *desc, gb_pet_sino_plan **plan);
+gb_status gb_pet_sino_plan_destroy(gb_pet_sino_plan *plan);
+/* Angle subsets i::n_subsets (pet_sinogram_system_matrix.py:131-144). */
+gb_status gb_pet_sino_set_subsets(gb_pet_sino_plan *plan, int32_t n_subsets);
+/* Angles in a subset (-1 = all angles). */
+int32_t gb_pet_sino_subset_size(const gb_pet_sino_plan *plan, int32_t subset);
+/* proj [n_sel][n_radial][n_planes] (x tof_num_bins, bin fastest, when use_tof on a TOF
+ * plan) = H img: joseph3d_fwd / joseph3d_fwd_tof_sino (:203-235). */
+gb_status gb_pet_sino_forward(gb_pet_sino_plan *plan, const float *img, float *proj,
+                              int32_t subset, int32_t use_tof, gb_stream_t stream);
+/* img = H^T proj (overwrites img): joseph3d_back / joseph3d_back_tof_sino (:263-292);
+ * use_tof = 0 on a TOF plan is the reference's force_nonTOF. */
+gb_status gb_pet_sino_backward(gb_pet_sino_plan *plan, const float *proj, float *img,
+                               int32_t subset, int32_t use_tof, gb_stream_t stream);
+/* prob [n_sel][n_radial][n_planes] = exp(-H mu), the attenuation probability sinogram
+ * (_compute_atteunation_probability_projection, :87-109). */
+gb_status gb_pet_sino_atten(gb_pet_sino_plan *plan, const float *mu, float *prob,
+                            int32_t subset, gb_stream_t stream);
+/* Listmode -> sinogram histogram (io/PET/shared.py:175-272), all pointers device:
+ * events [n_events][ncol] (id1, id2[, TOF bin]); weights [n_events] or NULL; lor_bins
+ * [ncpr][ncpr][2] (angular, radial) and plane_index [n_rings][n_rings] from
+ * sinogram_coordinates; tof_num_bins = 0 for a non-TOF sinogram; normalization averages the
+ * ordered and the mirrored binning.  sino [n_angles][n_radial][n_planes](x tof_num_bins) is
+ * overwritten. */
+gb_status gb_pet_lm_to_sino(const int32_t *events, int64_t n_events, int32_t ncol,
+                            const float *weights, const int32_t *lor_bins,
+                            const int32_t *plane_index, int32_t n_crystals_per_ring,
+                            int32_t n_rings, int32_t n_angles, int32_t n_radial,
+                            int32_t n_planes, int32_t tof_num_bins, int32_t normalization,
+                            float *sino, gb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

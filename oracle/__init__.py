@@ -49,6 +49,8 @@ def _lib(precision: str) -> ctypes.CDLL:
         lib.orc_pet_lm.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int64, P, P, P, P,
                                    P, ctypes.c_int, R, R, R, R, ctypes.c_int]
         lib.orc_pet_lor.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P, P, P, P, P]
+        lib.orc_pet_lor_tof.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P, P, P, P, P,
+                                        ctypes.c_int, R, R, R, R, ctypes.c_int]
         lib.orc_pad_size.argtypes = [ctypes.c_int]
         _libs[precision] = lib
     return _libs[precision]
@@ -301,6 +303,31 @@ class PetLMOracle:
         self.lib.orc_pet_lor(0, _ptr(xs), _ptr(xe), xs.shape[0], _ptr(img), _ptr(self.shape),
                              _ptr(self.origin), _ptr(self.vox), _ptr(out))
         return out
+
+    def lor_forward_tof(self, img, xs, xe):
+        """TOF sinogram projection of explicit LORs: [E, num_bins]."""
+        xs = np.ascontiguousarray(xs, self.dt); xe = np.ascontiguousarray(xe, self.dt)
+        img = np.ascontiguousarray(img, dtype=self.dt)
+        nb = int(self.tof[0])
+        out = np.zeros((xs.shape[0], nb), self.dt)
+        _, bw, sig, co, ns, shift = self._args()
+        R = self.dt
+        self.lib.orc_pet_lor_tof(0, _ptr(xs), _ptr(xe), xs.shape[0], _ptr(img), _ptr(self.shape),
+                                 _ptr(self.origin), _ptr(self.vox), _ptr(out), nb, R(bw), R(sig),
+                                 R(co), R(ns), shift)
+        return out
+
+    def lor_backward_tof(self, proj, xs, xe):
+        xs = np.ascontiguousarray(xs, self.dt); xe = np.ascontiguousarray(xe, self.dt)
+        nb = int(self.tof[0])
+        proj = np.ascontiguousarray(proj, self.dt).reshape(xs.shape[0], nb)
+        img = np.zeros(tuple(self.shape), self.dt)
+        _, bw, sig, co, ns, shift = self._args()
+        R = self.dt
+        self.lib.orc_pet_lor_tof(1, _ptr(xs), _ptr(xe), xs.shape[0], _ptr(img), _ptr(self.shape),
+                                 _ptr(self.origin), _ptr(self.vox), _ptr(proj), nb, R(bw), R(sig),
+                                 R(co), R(ns), shift)
+        return img
 
     def lor_backward(self, proj, xs, xe):
         xs = np.ascontiguousarray(xs, self.dt); xe = np.ascontiguousarray(xe, self.dt)

@@ -344,6 +344,27 @@ int orc_pet_lm(int back, const REAL *lut, const int64_t *ids, int ncol, int64_t 
     return 0;
 }
 
+/* TOF sinogram projector with explicit LOR endpoints xs/xe [E][3]: proj [E][nb], bin t
+ * centred as t - bin_shift (joseph3d_fwd_tof_sino / joseph3d_back_tof_sino call sites
+ * pet_sinogram_system_matrix.py:213-225, 271-284). */
+int orc_pet_lor_tof(int back, const REAL *xs, const REAL *xe, int64_t E, REAL *img,
+                    const int *n, const REAL *origin, const REAL *vox, REAL *proj, int nb,
+                    REAL bw, REAL sig, REAL center_offset, REAL n_sigmas, int bin_shift) {
+    #pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t e = 0; e < E; e++) {
+        for (int t = 0; t < nb; t++) {
+            REAL *pv = proj + e * nb + t;
+            if (back)
+                joseph(1, xs + 3 * e, xe + 3 * e, img, n, origin, vox, 1, bw, sig, center_offset,
+                       n_sigmas, t - bin_shift, *pv);
+            else
+                *pv = joseph(0, xs + 3 * e, xe + 3 * e, img, n, origin, vox, 1, bw, sig,
+                             center_offset, n_sigmas, t - bin_shift, 0);
+        }
+    }
+    return 0;
+}
+
 /* Same, with explicit LOR endpoints xs/xe [E][3] (used for sensitivity LOR sets). */
 int orc_pet_lor(int back, const REAL *xs, const REAL *xe, int64_t E, REAL *img, const int *n,
                 const REAL *origin, const REAL *vox, REAL *proj) {

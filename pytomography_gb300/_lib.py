@@ -58,6 +58,18 @@ class PetDesc(ctypes.Structure):
     ]
 
 
+class PetSinoDesc(ctypes.Structure):
+    _fields_ = [
+        ("nx", c_int), ("ny", c_int), ("nz", c_int),
+        ("vx", c_float), ("vy", c_float), ("vz", c_float),
+        ("ox", c_float), ("oy", c_float), ("oz", c_float),
+        ("n_angles", c_int), ("n_radial", c_int), ("n_planes", c_int),
+        ("det_xy", c_void_p), ("plane_z", c_void_p),
+        ("tof", c_int), ("tof_num_bins", c_int), ("tof_bin_width", c_float),
+        ("tof_sigma", c_float), ("tof_center_offset", c_float), ("tof_n_sigmas", c_float),
+    ]
+
+
 _LIB = None
 
 # (name, restype, argtypes) of every exported symbol declared in include/gbtomo.h
@@ -91,6 +103,16 @@ SIGNATURES = [
                                    c_float, c_void_p, c_void_p]),
     ("gb_pet_osem_step", c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_int64, c_void_p,
                                  c_void_p, c_int, c_void_p]),
+    ("gb_pet_sino_plan_create", c_int, [ctypes.POINTER(PetSinoDesc), ctypes.POINTER(c_void_p)]),
+    ("gb_pet_sino_plan_destroy", c_int, [c_void_p]),
+    ("gb_pet_sino_set_subsets", c_int, [c_void_p, c_int]),
+    ("gb_pet_sino_subset_size", c_int, [c_void_p, c_int]),
+    ("gb_pet_sino_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    ("gb_pet_sino_backward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    ("gb_pet_sino_atten", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("gb_pet_lm_to_sino", c_int, [c_void_p, ctypes.c_int64, c_int, c_void_p, c_void_p, c_void_p,
+                                  c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
+                                  c_void_p]),
 ]
 
 

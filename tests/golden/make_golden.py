@@ -188,6 +188,42 @@ def pet_meta_case(out):
     print("wrote pet_meta")
 
 
+def pet_sino_case(out):
+    """Sinogram geometry tables and listmode -> sinogram binning of a small scanner
+    (io/PET/shared.py:7-272)."""
+    set_precision(torch.float32)
+    info = dict(crystalTransNr=1, crystalTransSpacing=4.0, submoduleTransNr=1,
+                submoduleTransSpacing=0.0, moduleTransNr=1, moduleTransSpacing=0.0,
+                rsectorTransNr=60, crystalAxialNr=8, crystalAxialSpacing=4.0,
+                submoduleAxialNr=1, submoduleAxialSpacing=0.0, moduleAxialNr=1,
+                moduleAxialSpacing=0.0, rsectorAxialNr=1, radius=120.0,
+                firstCrystalAxis=1, NrCrystalsPerRing=60, NrRings=8, min_rsector_difference=0)
+    rec = {}
+    lor, sidx = pet_shared.sinogram_coordinates(info)
+    rec["lor_coordinates"] = lor.numpy()
+    rec["sinogram_index"] = sidx.numpy()
+    det, ring = pet_shared.sinogram_to_spatial(info)
+    rec["detector_coordinates"] = det.numpy()
+    rec["ring_coordinates"] = ring.numpy()
+    g = torch.Generator().manual_seed(31)
+    n_det = 60 * 8
+    ids = torch.randint(0, n_det, (4000, 2), generator=g)
+    ids = ids[ids[:, 0] != ids[:, 1]]
+    tof = torch.randint(0, 13, (ids.shape[0], 1), generator=g)
+    w = torch.rand(ids.shape[0], generator=g)
+    rec["events"] = torch.cat([ids, tof], 1).numpy()
+    rec["weights"] = w.numpy()
+    rec["sino"] = pet_shared.listmode_to_sinogram(ids, info).numpy()
+    rec["sino_w"] = pet_shared.listmode_to_sinogram(ids, info, weights=w).numpy()
+    rec["sino_norm"] = pet_shared.listmode_to_sinogram(ids, info, weights=w,
+                                                       normalization=True).numpy()
+    tm = PETTOFMeta(13, 650.0, 58.5)
+    rec["sino_tof"] = pet_shared.listmode_to_sinogram(torch.cat([ids, tof], 1), info,
+                                                      tof_meta=tm).numpy()
+    np.savez_compressed(os.path.join(out, "pet_sino.npz"), **rec)
+    print("wrote pet_sino", {k: v.shape for k, v in rec.items()})
+
+
 def theta_case(out):
     """Sampling matrices of the restated kornia rotation, for pinning the host tables."""
     rec = {}
@@ -265,6 +301,7 @@ def main():
               bsrem=True)
     rdp_case(out)
     pet_meta_case(out)
+    pet_sino_case(out)
     print("pad sizes", {n: compute_pad_size(n) for n in (15, 16, 64, 96, 128)})
 
 
