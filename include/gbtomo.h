@@ -280,6 +280,19 @@ gb_status gb_pet_lm_to_sino(const int32_t *events, int64_t n_events, int32_t nco
                             int32_t n_planes, int32_t tof_num_bins, int32_t normalization,
                             float *sino, gb_stream_t stream);
 
+/* ---------------------------------------------------- object-space operators */
+/* Separable Gaussian filter, GaussianFilter.forward (transforms/shared/filters.py:47-63):
+ * 'same' zero-padded correlation along x, then y, then z with odd tap counts.  All
+ * pointers device; in, out and scratch ([nx][ny][nz] each) must be distinct. */
+gb_status gb_filter3d(const float *in, float *out, float *scratch, int32_t nx, int32_t ny,
+                      int32_t nz, const float *taps_x, int32_t kx, const float *taps_y,
+                      int32_t ky, const float *taps_z, int32_t kz, gb_stream_t stream);
+/* Kernel-method basis, KEMTransform.forward (transforms/shared/kem.py:111-128):
+ * out[v] = sum_t kern[t][v] * in[clamp(v + offset_t)] over the size^3 offsets in
+ * (a, b, c) loop order, replicate boundary.  kern [size^3][nx][ny][nz] device. */
+gb_status gb_kem_apply(const float *in, float *out, const float *kern, int32_t nx, int32_t ny,
+                       int32_t nz, int32_t size, gb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,6 +110,10 @@ SIGNATURES = [
     ("gb_pet_sino_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
     ("gb_pet_sino_backward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
     ("gb_pet_sino_atten", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("gb_filter3d", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int,
+                            c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    ("gb_kem_apply", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                             c_void_p]),
     ("gb_pet_lm_to_sino", c_int, [c_void_p, ctypes.c_int64, c_int, c_void_p, c_void_p, c_void_p,
                                   c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
                                   c_void_p]),

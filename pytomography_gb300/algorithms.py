@@ -60,6 +60,7 @@ class PreconditionedGradientAscentAlgorithm:
               and (isinstance(sm, SPECTSystemMatrix)
                    or (isinstance(sm, PETLMSystemMatrix) and kind == "osem"
                        and not sm.scale_projection_by_sensitivity
+                       and not sm.obj2obj_transforms
                        and sm.output_device == sm.device)))
         if self._fused_request is True and not ok:
             raise NotImplementedError("this likelihood / system matrix / prior has no fused step")

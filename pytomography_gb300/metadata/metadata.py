@@ -7,6 +7,9 @@ class ObjectMeta:
 
     def __init__(self, dr, shape) -> None:
         self.dr = dr
+        self.dx = dr[0]
+        self.dy = dr[1]
+        self.dz = dr[2]
         self.shape = shape
 
 
@@ -15,3 +18,4 @@ class ProjMeta:
 
     def __init__(self, angles) -> None:
         self.angles = angles
+        self.num_projections = len(angles)

@@ -23,11 +23,12 @@ class PETLMSystemMatrix(SystemMatrix):
                  scale_projection_by_sensitivity: bool = False, N_splits: int = 1,
                  FOV_scale_enabled: bool = True, device=None,
                  compute_sensitivity: bool = True) -> None:
-        if obj2obj_transforms:
-            raise NotImplementedError("PET obj2obj transforms are not part of the fused path")
-        super().__init__(object_meta, proj_meta, [], [])
         if not torch.cuda.is_available():
             raise RuntimeError("PETLMSystemMatrix needs a CUDA device (no CPU path)")
+        # object-space transforms (e.g. GaussianFilter as the resolution model) run before
+        # forward projection and after back projection (petlm_system_matrix.py:258-260,
+        # 359-361); they disable the fused OSEM step
+        super().__init__(object_meta, proj_meta, obj2obj_transforms or [], [])
         self.device = torch.device("cuda", torch.cuda.current_device())
         self.output_device = self.device if device is None else torch.device(device)
         self.TOF = proj_meta.tof_meta is not None
@@ -152,6 +153,8 @@ class PETLMSystemMatrix(SystemMatrix):
         return self.get_projection_subset(self.proj_meta.weights, subset_idx).to(self.device)
 
     def forward(self, object, subset_idx=None):
+        for t in self.obj2obj_transforms:
+            object = t.forward(object)
         img = object.to(self.device, torch.float32).contiguous()
         out = torch.empty(self._n_sel(subset_idx), device=self.device)
         _lib.check(self._lib.gb_pet_forward(self._plan, _lib.ptr(img), _lib.ptr(out),
@@ -168,12 +171,16 @@ class PETLMSystemMatrix(SystemMatrix):
         out = torch.empty(tuple(self.object_meta.shape), device=self.device)
         _lib.check(self._lib.gb_pet_backward(self._plan, _lib.ptr(p), _lib.ptr(out),
                                              self._code(subset_idx), _lib.stream_handle(self.device)))
+        for t in self.obj2obj_transforms[::-1]:
+            out = t.backward(out)
         if return_norm_constant:
             return out.to(self.output_device), self.compute_normalization_factor(subset_idx)
         return out.to(self.output_device)
 
     def osem_step(self, object, numerator, additive, norm_bp, subset_idx):
         """Fused listmode OSEM sub-iteration in place on ``object``."""
+        if self.obj2obj_transforms:
+            raise NotImplementedError("the fused listmode step has no object-space transforms")
         num = numerator.to(self.device, torch.float32).contiguous()
         s = None if additive is None else additive.to(self.device, torch.float32).contiguous()
         _lib.check(self._lib.gb_pet_osem_step(self._plan, _lib.ptr(object), _lib.ptr(num),
@@ -201,6 +208,8 @@ class PETLMSystemMatrix(SystemMatrix):
         _lib.check(self._lib.gb_pet_sensitivity(self._plan, _lib.ptr(pairs), int(n_pairs),
                                                 _lib.ptr(w), _lib.ptr(mu), float(1e-11),
                                                 _lib.ptr(out), _lib.stream_handle(self.device)))
+        for t in self.obj2obj_transforms[::-1]:
+            out = t.backward(out)
         return out
 
 
@@ -218,11 +227,11 @@ class PETSinogramSystemMatrix(SystemMatrix):
                  sinogram_sensitivity: torch.Tensor | None = None,
                  scale_projection_by_sensitivity: bool = False, N_splits: int = 1,
                  device=None) -> None:
-        if obj2obj_transforms:
-            raise NotImplementedError("PET obj2obj transforms are not part of the fused path")
-        super().__init__(object_meta, proj_meta, [], [])
         if not torch.cuda.is_available():
             raise RuntimeError("PETSinogramSystemMatrix needs a CUDA device (no CPU path)")
+        # object-space transforms run before forward projection and after back projection
+        # (pet_sinogram_system_matrix.py:202-204, 293-295)
+        super().__init__(object_meta, proj_meta, obj2obj_transforms or [], [])
         self.device = torch.device("cuda", torch.cuda.current_device())
         self.output_device = self.device if device is None else torch.device(device)
         self.object_origin = (-np.array(object_meta.shape) / 2 + 0.5) * np.array(object_meta.dr)
@@ -345,6 +354,8 @@ class PETSinogramSystemMatrix(SystemMatrix):
 
     # ------------------------------------------------------------ projectors
     def forward(self, object, subset_idx=None):
+        for t in self.obj2obj_transforms:
+            object = t.forward(object)
         img = object.to(self.device, torch.float32).contiguous()
         out = torch.empty(self._sino_shape(subset_idx, self.TOF), device=self.device)
         _lib.check(self._lib.gb_pet_sino_forward(self._plan, _lib.ptr(img), _lib.ptr(out),
@@ -369,6 +380,8 @@ class PETSinogramSystemMatrix(SystemMatrix):
         _lib.check(self._lib.gb_pet_sino_backward(self._plan, _lib.ptr(p), _lib.ptr(out),
                                                   self._code(subset_idx), 1 if tof else 0,
                                                   _lib.stream_handle(self.device)))
+        for t in self.obj2obj_transforms[::-1]:
+            out = t.backward(out)
         return out
 
 

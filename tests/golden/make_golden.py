@@ -224,6 +224,56 @@ def pet_sino_case(out):
     print("wrote pet_sino", {k: v.shape for k, v in rec.items()})
 
 
+def kem_filter_case(out):
+    """GaussianFilter (transforms/shared/filters.py), KEMTransform (transforms/shared/kem.py)
+    and KEMSystemMatrix over a SPECT system matrix (projectors/shared/kem_system_matrix.py)."""
+    from pytomography.metadata import ObjectMeta
+    from pytomography.transforms.shared import GaussianFilter, KEMTransform
+    from pytomography.projectors.shared import KEMSystemMatrix
+    set_precision(torch.float32)
+    g = torch.Generator().manual_seed(41)
+    shape, dr = (14, 12, 10), (0.4, 0.5, 0.45)
+    om = ObjectMeta(list(dr), shape)
+    f = torch.rand(shape, generator=g) + 0.2
+    rec = {"object": f.numpy(), "shape": np.array(shape), "dr": np.array(dr)}
+    for fwhm, ns in ((1.2, 3.0), (0.7, 2.0)):
+        gf = GaussianFilter(fwhm, n_sigmas=ns)
+        gf.configure(om, None)
+        rec[f"gauss_{fwhm}_{ns}"] = gf(f.to(pt.device)).cpu().numpy()
+    s1 = torch.rand(shape, generator=g)
+    s2 = (torch.rand(shape, generator=g) > 0.5).to(torch.float32) * 3.0
+    rec["support1"], rec["support2"] = s1.numpy(), s2.numpy()
+    kem = KEMTransform([s1, s2], support_kernels_params=[[0.3], [1.0]],
+                       distance_kernel_params=[0.6], size=5)
+    kem.configure(om, None)
+    rec["kem_fwd"] = kem.forward(f.to(pt.device)).cpu().numpy()
+    kem3 = KEMTransform([s1], support_kernels_params=[[0.2]], distance_kernel_params=[0.5],
+                        size=3, top_N=10)
+    kem3.configure(om, None)
+    rec["kem3_top10_fwd"] = kem3.forward(f.to(pt.device)).cpu().numpy()
+    # KEM over a small SPECT system matrix with attenuation
+    sshape, sdr = (12, 12, 8), (0.48, 0.48, 0.48)
+    angles = [float(a) for a in np.linspace(0, 360, 9)[:-1]]
+    om2 = SPECTObjectMeta(list(sdr), sshape)
+    pm2 = SPECTProjMeta(sshape[1:], list(sdr[:2]), angles, radii=[20.0] * len(angles))
+    mu = torch.rand(sshape, generator=g) * 0.1
+    H = SPECTSystemMatrix([SPECTAttenuationTransform(mu.to(pt.device))], [], om2, pm2)
+    sup = torch.rand(sshape, generator=g)
+    kem2 = KEMTransform([sup], support_kernels_params=[[0.5]], distance_kernel_params=[1.0],
+                        size=3)
+    K = KEMSystemMatrix(H, kem2)
+    alpha = torch.rand(sshape, generator=g) + 0.1
+    proj = torch.rand((len(angles), *sshape[1:]), generator=g)
+    rec.update(spect_mu=mu.numpy(), spect_support=sup.numpy(), spect_angles=np.array(angles),
+               spect_alpha=alpha.numpy(), spect_proj=proj.numpy(),
+               kem_spect_fwd=K.forward(alpha.to(pt.device)).cpu().numpy(),
+               kem_spect_bwd=K.backward(proj.to(pt.device)).cpu().numpy())
+    K.set_n_subsets(2)
+    rec["kem_spect_norm1"] = K.compute_normalization_factor(1).cpu().numpy()
+    np.savez_compressed(os.path.join(out, "kem_filter.npz"), **rec)
+    print("wrote kem_filter", sorted(rec))
+
+
 def theta_case(out):
     """Sampling matrices of the restated kornia rotation, for pinning the host tables."""
     rec = {}
@@ -302,6 +352,7 @@ def main():
     rdp_case(out)
     pet_meta_case(out)
     pet_sino_case(out)
+    kem_filter_case(out)
     print("pad sizes", {n: compute_pad_size(n) for n in (15, 16, 64, 96, 128)})
 
 
