@@ -169,6 +169,13 @@ gb_status gb_spect_bsrem_step(gb_spect_plan *plan, const float *object_in, float
 gb_status gb_rdp_gradient(const float *object, float *grad, int32_t nx, int32_t ny,
                           int32_t nz, float dx, float dy, float dz, const gb_rdp_desc *prior,
                           float beta_scale, gb_stream_t stream);
+/* RDP second derivative at f applied to x (the derivative_order=2 operator of
+ * NearestNeighbourPrior.__call__, nearest_neighbour.py:89-110 with phi2_1 / phi2_2 of
+ * :179-183): out_r = beta * scale * fov_r * sum_s w_rs (phi2_1(f_r, f_s) x_r +
+ * phi2_2(f_r, f_s) x_s); used by the uncertainty estimate.  out must not alias f or x. */
+gb_status gb_rdp_hessian_vector(const float *f, const float *x, float *out, int32_t nx,
+                                int32_t ny, int32_t nz, float dx, float dy, float dz,
+                                const gb_rdp_desc *prior, float beta_scale, gb_stream_t stream);
 
 /* -------------------------------------------------------------------- PET */
 

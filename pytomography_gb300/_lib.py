@@ -93,6 +93,9 @@ SIGNATURES = [
                                     c_float, c_int, c_void_p]),
     ("gb_rdp_gradient", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_float,
                                 c_float, ctypes.POINTER(RdpDesc), c_float, c_void_p]),
+    ("gb_rdp_hessian_vector", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_float,
+                                      c_float, c_float, ctypes.POINTER(RdpDesc), c_float,
+                                      c_void_p]),
     ("gb_pet_plan_create", c_int, [ctypes.POINTER(PetDesc), ctypes.POINTER(c_void_p)]),
     ("gb_pet_plan_destroy", c_int, [c_void_p]),
     ("gb_pet_set_subsets", c_int, [c_void_p, c_int]),

@@ -69,6 +69,76 @@ class PreconditionedGradientAscentAlgorithm:
     def _fused_kind(self):
         return None
 
+    # ------------------------------------------------------------ uncertainty
+    def compute_uncertainty(self, mask: torch.Tensor, data_storage_callback,
+                            subiteration_number: int | None = None, return_pct: bool = False,
+                            include_additive_term: bool = False, post_recon_filter=None):
+        """Uncertainty of the sum of counts in ``mask`` from the iterates stored by a
+        ``DataStorageCallback`` (preconditioned_gradient_ascent.py:170-215): the
+        variance propagates back through every sub-iteration with the operators Q and B,
+        whose projector calls run on the GPU kernels."""
+        cb = data_storage_callback
+        if subiteration_number is None:
+            subiteration_number = len(cb.objects) - 1
+        final_recon = cb.objects[subiteration_number].to(_p.device)
+        if post_recon_filter is not None:
+            Q = post_recon_filter(mask)
+            final_recon = post_recon_filter(final_recon)
+        else:
+            Q = mask.clone()
+        V = 0
+        for n in range(subiteration_number, 0, -1):
+            V = V + self._compute_B(Q, cb, n - 1, include_additive_term=include_additive_term)
+            if n > 1:
+                Q = self._compute_Q(Q, cb, n - 1)
+        abs2 = torch.sum(V[0] * self.likelihood.projections * V[0])
+        if include_additive_term:
+            abs2 = abs2 + torch.sum(self.likelihood.additive_term_variance_estimate(V[1]))
+        unc_abs = torch.sqrt(abs2).item()
+        if not return_pct:
+            return unc_abs
+        return unc_abs, unc_abs / (final_recon * mask).sum().item() * 100
+
+    def _uncertainty_subset(self, n: int):
+        return None if self.n_subsets == 1 else n % self.n_subsets
+
+    def _compute_Q(self, input, cb, n: int):
+        """Q of the uncertainty recursion (preconditioned_gradient_ascent.py:217-251)."""
+        subset_idx = self._uncertainty_subset(n)
+        f_n = cb.objects[n].to(_p.device)
+        f_next = cb.objects[n + 1].to(_p.device)
+        fp_n = cb.projections_predicted[n].to(_p.device)
+        grad_ff = self.likelihood.compute_gradient_ff(f_n, fp_n, subset_idx)
+        out = input * f_n * self._linear_preconditioner_factor(None, subset_idx)
+        if self.prior is not None:
+            self.prior.set_beta_scale(self.likelihood.system_matrix.get_weighting_subset(subset_idx))
+            self.prior.set_object(f_n)
+            out = grad_ff(out) - self.prior(derivative_order=2)(out)
+        else:
+            out = grad_ff(out)
+        return out + (f_next / (f_n + _p.delta)) * input
+
+    def _compute_B(self, input, cb, n: int, include_additive_term: bool = False):
+        """B of the uncertainty recursion (preconditioned_gradient_ascent.py:253-299)."""
+        sm = self.likelihood.system_matrix
+        subset_idx = self._uncertainty_subset(n)
+        if subset_idx is None:
+            rows = torch.arange(sm.proj_meta.shape[0]).to(torch.long).to(_p.device)
+        else:
+            rows = sm.subset_indices_array[subset_idx]
+        f_n = cb.objects[n].to(_p.device)
+        fp_n = cb.projections_predicted[n].to(_p.device)
+        out = input * f_n * self._linear_preconditioner_factor(None, subset_idx)
+        primary = self.likelihood.compute_gradient_gf(f_n, fp_n, subset_idx)(out)
+        n_out = 2 if include_additive_term else 1
+        total = torch.zeros((n_out, *fp_n.shape[:-3], *sm.proj_meta.shape[-3:]),
+                            device=primary.device)
+        total[0, ..., rows, :, :] = primary
+        if include_additive_term:
+            total[1, ..., rows, :, :] = self.likelihood.compute_gradient_sf(f_n, fp_n,
+                                                                            subset_idx)(out)
+        return total
+
     def _fused_begin(self) -> None:
         pass
 
@@ -170,6 +240,8 @@ class BSREM(LinearPreconditionedGradientAscentAlgorithm):
 
     def _fused_kind(self):
         from .priors import RelativeDifferencePrior
+        if getattr(getattr(self, "callback", None), "needs_projections_predicted", False):
+            return None  # the fused BSREM step keeps its predicted projections inside
         if self.prior is None or isinstance(self.prior, RelativeDifferencePrior):
             return "bsrem"
         return None

@@ -413,6 +413,50 @@ __global__ void k_rdp(const float *__restrict__ f, float *__restrict__ grad, int
     grad[i] = v;
 }
 
+// Second derivative of the RDP applied to x (nearest_neighbour.py:89-110, 173-177):
+// out_r = beta s FOV_r sum_s w_rs (phi2_1(f_r, f_s) x_r + phi2_2(f_r, f_s) x_s) with
+// phi2_1 = 2 (2 f_s + delta)^2 / D^3, phi2_2 = -2 (2 f_r + delta)(2 f_s + delta) / D^3,
+// D = gamma |f_r - f_s| + f_r + f_s + delta, replicate boundary.
+__global__ void k_rdp_hvp(const float *__restrict__ f, const float *__restrict__ xin,
+                          float *__restrict__ out, int nx, int ny, int nz, UpdateArgs u,
+                          float scale) {
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)nx * ny * nz) return;
+    const int z = idx % nz, y = (idx / nz) % ny, x = idx / ((size_t)nz * ny);
+    const float fr = f[idx], xr = xin[idx];
+    float diag = 0.f, off = 0.f;
+    int n = 0;
+    for (int i = -1; i <= 1; i++) {
+        const int xi = min(max(x + i, 0), nx - 1);
+        for (int j = -1; j <= 1; j++) {
+            const int yj = min(max(y + j, 0), ny - 1);
+            for (int k = -1; k <= 1; k++) {
+                if (i == 0 && j == 0 && k == 0) continue;
+                const int zk = min(max(z + k, 0), nz - 1);
+                const size_t o = ((size_t)xi * ny + yj) * nz + zk;
+                const float fs = __ldg(f + o), xs = __ldg(xin + o);
+                const float D = u.gamma * fabsf(fr - fs) + fr + fs + u.rdelta;
+                const float D3 = D * D * D;
+                const float as = 2.f * fs + u.rdelta, ar = 2.f * fr + u.rdelta;
+                diag += u.w26[n] * (2.f * as * as / D3);
+                off += u.w26[n] * (-2.f * ar * as / D3) * xs;
+                n++;
+            }
+        }
+    }
+    float v = scale * (diag * xr + off);
+    if (u.fov) v *= u.fov[idx];
+    out[idx] = v;
+}
+
+cudaError_t launch_rdp_hvp(const float *f, const float *x, float *out, int nx, int ny, int nz,
+                           const UpdateArgs &u, float beta_scale, cudaStream_t st) {
+    size_t n = (size_t)nx * ny * nz;
+    k_rdp_hvp<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(f, x, out, nx, ny, nz, u,
+                                                          u.beta * beta_scale);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rdp(const float *f, float *grad, int nx, int ny, int nz, const UpdateArgs &u,
                        float beta_scale, cudaStream_t st) {
     size_t n = (size_t)nx * ny * nz;

@@ -44,6 +44,8 @@ cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_ang
                          cudaStream_t st);
 cudaError_t launch_rdp(const float *f, float *grad, int nx, int ny, int nz, const UpdateArgs &u,
                        float beta_scale, cudaStream_t st);
+cudaError_t launch_rdp_hvp(const float *f, const float *x, float *out, int nx, int ny, int nz,
+                           const UpdateArgs &u, float beta_scale, cudaStream_t st);
 
 // Launch geometry of one forward projection of a plan (for entry points defined outside
 // spect_plan.cu): false when the subset is out of range.

@@ -892,6 +892,24 @@ gb_status gb_rdp_gradient(const float *f, float *grad, int32_t nx, int32_t ny, i
     return GB_OK;
 }
 
+gb_status gb_rdp_hessian_vector(const float *f, const float *x, float *out, int32_t nx,
+                                int32_t ny, int32_t nz, float dx, float dy, float dz,
+                                const gb_rdp_desc *prior, float beta_scale, gb_stream_t stream) {
+    clear_error();
+    GB_CHECK_ARG(f && x && out && prior, "null argument");
+    GB_CHECK_ARG(nx > 0 && ny > 0 && nz > 0, "shape must be positive");
+    GB_CHECK_ARG(out != f && out != x, "out must not alias f or x");
+    UpdateArgs u{};
+    u.prior = 1;
+    u.beta = prior->beta;
+    u.gamma = prior->gamma;
+    u.rdelta = prior->delta;
+    u.fov = prior->fov_scale;
+    rdp_weights(dx, dy, dz, u.w26);
+    GB_CUDA(launch_rdp_hvp(f, x, out, nx, ny, nz, u, beta_scale, as_stream(stream)));
+    return GB_OK;
+}
+
 }  // extern "C"
 
 namespace gb {

@@ -101,9 +101,27 @@ class RelativeDifferencePrior(Prior):
                     tot += (phi * float(self.weight((i, j, k))) * self.FOV_scale).sum()
         return float(self.beta * tot)
 
+    def hessian_vector(self, x: torch.Tensor, beta_scale: float = 1.0) -> torch.Tensor:
+        """Second derivative at the current object applied to ``x``
+        (gb_rdp_hessian_vector)."""
+        lib = _lib.load()
+        f = self.object.to(torch.float32).contiguous()
+        _lib.require_cuda(f, "object")
+        xv = x.to(f.device, torch.float32).contiguous()
+        out = torch.empty_like(f)
+        d = self._desc()
+        dx, dy, dz = (float(v) for v in self.object_meta.dr)
+        _lib.check(lib.gb_rdp_hessian_vector(_lib.ptr(f), _lib.ptr(xv), _lib.ptr(out), *f.shape,
+                                             dx, dy, dz, ctypes.byref(d), float(beta_scale),
+                                             _lib.stream_handle(f.device)))
+        return out
+
     def __call__(self, derivative_order: int = 0):
         if derivative_order == 0:
             return self._value()
         if derivative_order == 1:
             return self.gradient(self.object, self.beta_scale_factor)
-        raise NotImplementedError("second-order RDP derivatives are outside the fused path")
+        if derivative_order == 2:  # an operator, as in nearest_neighbour.py:105-108
+            scale = self.beta_scale_factor
+            return lambda x: self.hessian_vector(x, scale)
+        raise NotImplementedError("prior derivatives of order > 2 are not defined")

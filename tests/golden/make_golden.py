@@ -274,6 +274,49 @@ def kem_filter_case(out):
     print("wrote kem_filter", sorted(rec))
 
 
+def uncertainty_case(out):
+    """compute_uncertainty over a DataStorageCallback (preconditioned_gradient_ascent.py:
+    170-299, callbacks/data_saving.py) for OSEM, OSEM with a post-reconstruction Gaussian
+    filter, and BSREM with the RDP prior (its second derivative)."""
+    from pytomography.callbacks import DataStorageCallback
+    from pytomography.transforms.shared import GaussianFilter
+    shape, dr = (16, 16, 10), (0.48, 0.48, 0.48)
+    angles = [float(a) for a in np.linspace(0, 360, 13)[:-1]]
+    radius, seed = 20.0, 51
+    f_true, mu_np = ellipsoid_phantom(shape, dr, seed, n_ell=2)
+    set_precision(torch.float32)
+    om = SPECTObjectMeta(list(dr), tuple(shape))
+    pm = SPECTProjMeta((shape[1], shape[2]), list(dr[:2]), angles, radii=[radius] * len(angles))
+    H = SPECTSystemMatrix([SPECTAttenuationTransform(torch.tensor(mu_np, dtype=torch.float32)),
+                           SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)))], [], om, pm)
+    g = torch.poisson(H.forward(torch.tensor(f_true, dtype=torch.float32)) * 20,
+                      generator=torch.Generator().manual_seed(seed + 1))
+    mask = torch.zeros(shape, dtype=torch.bool)
+    mask[5:11, 4:10, 3:7] = True
+    rec = {"shape": np.array(shape), "dr": np.array(dr), "angles": np.array(angles),
+           "radius": radius, "mu": mu_np, "projections": g.numpy(), "mask": mask.numpy()}
+    for name, bsrem in (("osem", False), ("bsrem", True)):
+        lik = PoissonLogLikelihood(H, g)
+        if bsrem:
+            alg = BSREM(lik, prior=RelativeDifferencePrior(beta=0.3, gamma=2))
+        else:
+            alg = OSEM(lik)
+        cb = DataStorageCallback(lik, torch.clone(alg.object_prediction))
+        recon = alg(2, 3, callback=cb)
+        rec[f"{name}_recon"] = recon.numpy()
+        a_abs, a_pct = alg.compute_uncertainty(mask, cb, return_pct=True)
+        rec[f"{name}_unc"] = np.array([a_abs, a_pct])
+        rec[f"{name}_unc_sub3"] = np.array(alg.compute_uncertainty(mask, cb, subiteration_number=3))
+        if not bsrem:
+            gf = GaussianFilter(0.8)
+            gf.configure(om, pm)
+            # the filter convolves the mask, so it has to be a float mask
+            rec["osem_unc_filtered"] = np.array(alg.compute_uncertainty(
+                mask.to(torch.float32), cb, post_recon_filter=gf))
+    np.savez_compressed(os.path.join(out, "uncertainty.npz"), **rec)
+    print("wrote uncertainty", {k: v for k, v in rec.items() if k.endswith(("unc", "sub3", "filtered"))})
+
+
 def theta_case(out):
     """Sampling matrices of the restated kornia rotation, for pinning the host tables."""
     rec = {}
@@ -353,6 +396,7 @@ def main():
     pet_meta_case(out)
     pet_sino_case(out)
     kem_filter_case(out)
+    uncertainty_case(out)
     print("pad sizes", {n: compute_pad_size(n) for n in (15, 16, 64, 96, 128)})
 
 
