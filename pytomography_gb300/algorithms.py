@@ -265,3 +265,114 @@ class BSREM(LinearPreconditionedGradientAscentAlgorithm):
                       subset_idx=subset_idx)
         self._pingpong = self.object_prediction
         self.object_prediction = out
+
+
+class PGAAMultiBedSPECT(PreconditionedGradientAscentAlgorithm):
+    """Multi-bed SPECT: one reconstruction algorithm per bed position, sub-iteration by
+    sub-iteration, stitched after every sub-iteration (preconditioned_gradient_ascent.py:
+    550-663).
+
+    ``files_NM`` of the reference are DICOM files whose headers give each bed's z
+    position; here pass the z positions (``bed_z``, any length unit) and the slice spacing
+    in the same unit.  When every bed runs fused OSEM on a SPECT system matrix and no
+    callback is given, the beds' sub-iterations run together as CUDA graphs
+    (``BatchedOSEM``); the iterates are the same as bed by bed.
+    """
+
+    def __init__(self, bed_z, reconstruction_algorithms, slice_spacing: float | None = None,
+                 batched: bool = True) -> None:
+        if any(isinstance(b, str) for b in bed_z):
+            raise NotImplementedError("DICOM headers are not read here: pass the beds' z "
+                                      "positions and slice_spacing")
+        if slice_spacing is None:
+            raise ValueError("slice_spacing is required with explicit bed positions")
+        self.bed_z = [float(b) for b in bed_z]
+        self.slice_spacing = float(slice_spacing)
+        self.reconstruction_algorithms = list(reconstruction_algorithms)
+        self.batched = batched
+
+    def _stitch(self, recons):
+        from .io.SPECT import stitch_multibed
+        return stitch_multibed(torch.stack(recons), self.bed_z, self.slice_spacing)
+
+    def _batch(self, n_subsets):
+        from .batched import BatchedOSEM
+        from .projectors.SPECT import SPECTSystemMatrix
+        algs = self.reconstruction_algorithms
+        ok = self.batched and all(
+            type(a) is OSEM and a._fused_request is not False
+            and type(a.likelihood) is PoissonLogLikelihood
+            and isinstance(a.likelihood.system_matrix, SPECTSystemMatrix) for a in algs)
+        if not ok:
+            return None
+        return BatchedOSEM([a.likelihood for a in algs], n_subsets=n_subsets,
+                           object_initial=[a.object_prediction for a in algs])
+
+    def __call__(self, n_iters: int, n_subsets: int, callback=None) -> torch.Tensor:
+        self.callback = callback
+        batch = self._batch(n_subsets) if callback is None else None
+        for i in range(n_iters):
+            for j in range(n_subsets):
+                if batch is not None:
+                    batch.step(j)
+                    self.recons = batch.objects
+                else:
+                    self.recons = [a(1, n_subsets, n_subset_specific=j)
+                                   for a in self.reconstruction_algorithms]
+                self.object_prediction = self._stitch(self.recons)
+                self._multibed_callback(i, j)
+        if batch is not None:
+            for a, f in zip(self.reconstruction_algorithms, batch.objects):
+                a.object_prediction = f.clone()
+        self._finalize_callback()
+        return self.object_prediction
+
+    def _multibed_callback(self, n_iter: int, n_subset: int) -> None:
+        if self.callback is None:
+            return
+        if isinstance(self.callback, list):
+            for a, cb in zip(self.reconstruction_algorithms, self.callback):
+                a.callback = cb
+                a._compute_callback(n_iter=n_iter, n_subset=n_subset)
+        else:
+            self.object_prediction = self.callback.run(self.object_prediction, n_iter, n_subset)
+
+    def _finalize_callback(self) -> None:
+        if self.callback is None:
+            return
+        if isinstance(self.callback, list):
+            for a, cb in zip(self.reconstruction_algorithms, self.callback):
+                a.callback = cb
+                cb.finalize(a.object_prediction)
+        else:
+            self.callback.finalize(self.object_prediction)
+
+    def compute_uncertainty(self, mask: torch.Tensor, data_storage_callbacks,
+                            subiteration_number: int | None = None, return_pct: bool = False,
+                            include_additive_term: bool = False):
+        """Uncertainty of the counts in ``mask`` (stitched-image shape): each bed's share
+        of the mask, weighted by that bed's own stitching weights, goes through the bed's
+        ``compute_uncertainty`` and the results add in quadrature
+        (preconditioned_gradient_ascent.py:623-663).  The reference weights every bed with
+        the first bed's profile (its stitching helper concatenates the weights instead of
+        stacking them); each bed's own weights are used here."""
+        from .io.SPECT import stitch_multibed
+        if subiteration_number is None:
+            subiteration_number = len(data_storage_callbacks[0].objects) - 1
+        recons = [cb.objects[subiteration_number].to(_p.device) for cb in data_storage_callbacks]
+        weights, zs = stitch_multibed(torch.stack(recons), self.bed_z, self.slice_spacing,
+                                      return_stitching_weights=True)
+        unc, total = [], 0.0
+        lz = recons[0].shape[-1]
+        for k in range(len(recons)):
+            mask_k = mask[:, :, zs[k]:zs[k] + lz] * weights[k]
+            if mask_k.sum() == 0:
+                continue
+            unc.append(self.reconstruction_algorithms[k].compute_uncertainty(
+                mask_k, data_storage_callbacks[k], subiteration_number, return_pct=False,
+                include_additive_term=include_additive_term))
+            total += (recons[k] * mask_k).sum().item()
+        unc_abs = torch.sqrt(torch.sum(torch.tensor(unc) ** 2)).item()
+        if return_pct:
+            return unc_abs, unc_abs / total * 100
+        return unc_abs

@@ -317,6 +317,50 @@ def uncertainty_case(out):
     print("wrote uncertainty", {k: v for k, v in rec.items() if k.endswith(("unc", "sub3", "filtered"))})
 
 
+def multibed_case(out):
+    """PGAAMultiBedSPECT (preconditioned_gradient_ascent.py:550-600) over three bed positions
+    with stitch_multibed (io/SPECT/dicom.py:599-653).  The bed z positions and slice spacing
+    that the reference reads from DICOM headers are given by stand-in header objects."""
+    from pytomography.algorithms import PGAAMultiBedSPECT
+    from pytomography.io.SPECT import dicom as ref_dicom
+    shape, dr = (16, 16, 10), (0.48, 0.48, 0.48)
+    angles = [float(a) for a in np.linspace(0, 360, 13)[:-1]]
+    z_mm = [57.6, 0.0, 28.8]  # unsorted on purpose: the stitching sorts by z
+    spacing_mm = 4.8
+
+    class _Pos:
+        def __init__(self, z):
+            self.ImagePositionPatient = [0.0, 0.0, z]
+
+    class _Header:
+        def __init__(self, z):
+            self.DetectorInformationSequence = [_Pos(z)]
+            self.PixelSpacing = [spacing_mm, spacing_mm]
+            self.Rows = shape[0]
+
+    headers = {f"bed{i}": _Header(z) for i, z in enumerate(z_mm)}
+    ref_dicom.pydicom.dcmread = lambda f: headers[f]
+    set_precision(torch.float32)
+    rec = {"shape": np.array(shape), "dr": np.array(dr), "angles": np.array(angles),
+           "z_mm": np.array(z_mm), "spacing_mm": spacing_mm}
+    algs = []
+    for b in range(3):
+        f_true, mu_np = ellipsoid_phantom(shape, dr, 60 + b, n_ell=2)
+        om = SPECTObjectMeta(list(dr), shape)
+        pm = SPECTProjMeta(shape[1:], list(dr[:2]), angles, radii=[20.0] * len(angles))
+        H = SPECTSystemMatrix([SPECTAttenuationTransform(torch.tensor(mu_np, dtype=torch.float32)),
+                               SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)))], [], om, pm)
+        g = torch.poisson(H.forward(torch.tensor(f_true, dtype=torch.float32)) * 20,
+                          generator=torch.Generator().manual_seed(70 + b))
+        rec[f"mu{b}"], rec[f"proj{b}"] = mu_np, g.numpy()
+        algs.append(OSEM(PoissonLogLikelihood(H, g)))
+    mb = PGAAMultiBedSPECT([f"bed{i}" for i in range(3)], algs)
+    rec["stitched"] = mb(2, 3).numpy()
+    rec["beds"] = np.stack([a.object_prediction.numpy() for a in algs])
+    np.savez_compressed(os.path.join(out, "multibed.npz"), **rec)
+    print("wrote multibed", rec["stitched"].shape)
+
+
 def theta_case(out):
     """Sampling matrices of the restated kornia rotation, for pinning the host tables."""
     rec = {}
@@ -397,6 +441,7 @@ def main():
     pet_sino_case(out)
     kem_filter_case(out)
     uncertainty_case(out)
+    multibed_case(out)
     print("pad sizes", {n: compute_pad_size(n) for n in (15, 16, 64, 96, 128)})
 
 
