@@ -3,15 +3,38 @@
 //
 // Tap tiers: a plane whose kernel is narrow (its outer taps are exactly zero, or below
 // the plan's truncation threshold) runs a shorter unrolled loop.  A plane of bucket K
-// (half width H) uses KK = 2h+1 taps with h = H/2, 3H/4 or H (tiers 0, 1, 2); the taps
-// used are the centred KK of the K stored.
+// (half width H) uses KK = 2h+1 taps with h = round(H * {0.2, 0.35, 0.5, 0.65, 0.8, 1})
+// (tiers 0..5; h = 3, 5, 7, 9, 11, 14 for K = 29); the taps used are the centred KK of
+// the K stored.
 #pragma once
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 namespace gb {
 
+constexpr int kTiers = 6;
+
 __host__ __device__ constexpr int tier_half(int K, int tier) {
-    return tier == 0 ? (K / 2) / 2 : (tier == 1 ? (3 * (K / 2)) / 4 : K / 2);
+    return tier >= kTiers - 1
+               ? K / 2
+               : ((K / 2) * (tier == 0 ? 4 : tier == 1 ? 7 : tier == 2 ? 10 : tier == 3 ? 13 : 16) +
+                  10) / 20;
+}
+
+__host__ __device__ constexpr int tier_taps(int K, int tier) { return 2 * tier_half(K, tier) + 1; }
+
+// Calls f(std::integral_constant<int, KK>) with the tap count of the plane's tier.
+template <int K, typename F>
+__device__ __forceinline__ void tier_dispatch(int tier, F &&f) {
+    switch (tier) {
+        case 0: f(std::integral_constant<int, tier_taps(K, 0)>{}); break;
+        case 1: f(std::integral_constant<int, tier_taps(K, 1)>{}); break;
+        case 2: f(std::integral_constant<int, tier_taps(K, 2)>{}); break;
+        case 3: f(std::integral_constant<int, tier_taps(K, 3)>{}); break;
+        case 4: f(std::integral_constant<int, tier_taps(K, 4)>{}); break;
+        default: f(std::integral_constant<int, K>{}); break;
+    }
 }
 
 // First pass: blur along the S row axis for output row blocks [b_lo, b_hi) and columns
@@ -62,6 +85,22 @@ __device__ __forceinline__ void blur_second(const float *__restrict__ Tt,
     for (int i = 0; i < OB + KK - 1; i++) win[i] = tq[i * TS];
 #pragma unroll
     for (int j = 0; j < OB; j++) o[j] = 0.f;
+#pragma unroll
+    for (int t = 0; t < KK; t++)
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
+}
+
+// Same as blur_second, accumulating into o (o += blur) instead of overwriting it.
+template <int K, int KK, int OB>
+__device__ __forceinline__ void blur_second_acc(const float *__restrict__ Tt,
+                                                const float (&w)[KK], int TS, int row0, int col,
+                                                float (&o)[OB]) {
+    constexpr int OFF = (K - KK) / 2;
+    const float *tq = Tt + (row0 + OFF) * TS + col;
+    float win[OB + KK - 1];
+#pragma unroll
+    for (int i = 0; i < OB + KK - 1; i++) win[i] = tq[i * TS];
 #pragma unroll
     for (int t = 0; t < KK; t++)
 #pragma unroll

@@ -157,17 +157,14 @@ __global__ void __launch_bounds__(512, 1)
             GB_B1T(1, t1 - t0);
             t0 = t1;
         }
-        constexpr int KK0 = 2 * tier_half(K, 0) + 1, KK1 = 2 * tier_half(K, 1) + 1;
-        int tier = 2;
-        if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : 2;
-        if (tier == 0)
-            blur_first<K, KK0, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
-        else if (tier == 1)
-            blur_first<K, KK1, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
-        else
-            blur_first<K, K, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        int tier = kTiers - 1;
+        if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : kTiers - 1;
+        tier_dispatch<K>(tier, [&](auto kk) {
+            constexpr int KK = decltype(kk)::value;
+            blur_first<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+        });
         GB_B1T(6, rb - ra + 1);
-        GB_B1T(7, (rb - ra + 1) * (tier == 0 ? KK0 : (tier == 1 ? KK1 : K)));
+        GB_B1T(7, (rb - ra + 1) * tier_taps(K, tier));
         __syncthreads();
         {
             long long t1 = GB_B1NOW();
@@ -179,62 +176,60 @@ __global__ void __launch_bounds__(512, 1)
             const bool amul = Ap && g.att_first;
             // warp-tasks (32-row chunk, z block); lanes take consecutive output rows
             const int nrc = ((b_hi - b_lo) * OB + 31) >> 5;
-#define GB_B1_PHASE3(KK)                                                                     \
-    {                                                                                        \
-        float w[KK];                                                                         \
-        load_taps<K, KK>(tap + K, w);                                                        \
-        for (int p = warp; p < nrc * (Z8 / OB); p += nwarp) {                                \
-            const int rc = p % nrc, zb = p / nrc;                                            \
-            const int o_row = b_lo * OB + (rc << 5) + lane;                                  \
-            if (o_row >= b_hi * OB) continue;                                                \
-            const int y = g.pad - H + o_row;                                                 \
-            const bool store = y >= ra && y <= rb;                                           \
-            const int zl0 = zb * OB;                                                         \
-            const bool full = VEC && (zl0 + OB <= Zc);                                       \
-            const size_t rowoff = (size_t)(y - g.ya_lo) * nz + z0 + zl0;                     \
-            float av[OB];                                                                    \
-            if (store && amul) { /* issue the A loads before the blur arithmetic */          \
-                if (full) {                                                                  \
-                    _Pragma("unroll") for (int j = 0; j < OB; j += 4) {                      \
-                        float4 a4 = __ldg(reinterpret_cast<const float4 *>(Ap + rowoff + j)); \
-                        av[j] = a4.x;                                                        \
-                        av[j + 1] = a4.y;                                                    \
-                        av[j + 2] = a4.z;                                                    \
-                        av[j + 3] = a4.w;                                                    \
-                    }                                                                        \
-                } else {                                                                     \
-                    _Pragma("unroll") for (int j = 0; j < OB; j++) av[j] =                   \
-                        zl0 + j < Zc ? Ap[rowoff + j] : 0.f;                                 \
-                }                                                                            \
-            }                                                                                \
-            float o[OB];                                                                     \
-            if (g.psf2d) {                                                                   \
-                blur_second<K, KK, OB>(Tt, w, TS, zb * OB, o_row, o);                        \
-            } else {                                                                         \
-                _Pragma("unroll") for (int j = 0; j < OB; j++) o[j] =                        \
-                    Tt[(zb * OB + j + H) * TS + o_row];                                      \
-            }                                                                                \
-            if (!store) continue;                                                            \
-            if (amul) {                                                                      \
-                _Pragma("unroll") for (int j = 0; j < OB; j++) o[j] = __fmul_rn(o[j], av[j]); \
-            }                                                                                \
-            if (full) {                                                                      \
-                _Pragma("unroll") for (int j = 0; j < OB; j += 4)                            \
-                    *reinterpret_cast<float4 *>(Wp + rowoff + j) =                           \
-                        make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);                     \
-            } else {                                                                         \
-                _Pragma("unroll") for (int j = 0; j < OB; j++) if (zl0 + j < Zc)             \
-                    Wp[rowoff + j] = o[j];                                                   \
-            }                                                                                \
-        }                                                                                    \
-    }
-            if (tier == 0)
-                GB_B1_PHASE3(KK0)
-            else if (tier == 1)
-                GB_B1_PHASE3(KK1)
-            else
-                GB_B1_PHASE3(K)
-#undef GB_B1_PHASE3
+            tier_dispatch<K>(tier, [&](auto kk) {
+                constexpr int KK = decltype(kk)::value;
+                float w[KK];
+                load_taps<K, KK>(tap + K, w);
+                for (int p = warp; p < nrc * (Z8 / OB); p += nwarp) {
+                    const int rc = p % nrc, zb = p / nrc;
+                    const int o_row = b_lo * OB + (rc << 5) + lane;
+                    if (o_row >= b_hi * OB) continue;
+                    const int y = g.pad - H + o_row;
+                    const bool store = y >= ra && y <= rb;
+                    const int zl0 = zb * OB;
+                    const bool full = VEC && (zl0 + OB <= Zc);
+                    const size_t rowoff = (size_t)(y - g.ya_lo) * nz + z0 + zl0;
+                    float av[OB];
+                    if (store && amul) {  // issue the A loads before the blur arithmetic
+                        if (full) {
+#pragma unroll
+                            for (int j = 0; j < OB; j += 4) {
+                                const float4 a4 =
+                                    __ldg(reinterpret_cast<const float4 *>(Ap + rowoff + j));
+                                av[j] = a4.x;
+                                av[j + 1] = a4.y;
+                                av[j + 2] = a4.z;
+                                av[j + 3] = a4.w;
+                            }
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < OB; j++) av[j] = zl0 + j < Zc ? Ap[rowoff + j] : 0.f;
+                        }
+                    }
+                    float o[OB];
+                    if (g.psf2d) {
+                        blur_second<K, KK, OB>(Tt, w, TS, zb * OB, o_row, o);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + H) * TS + o_row];
+                    }
+                    if (!store) continue;
+                    if (amul) {
+#pragma unroll
+                        for (int j = 0; j < OB; j++) o[j] = __fmul_rn(o[j], av[j]);
+                    }
+                    if (full) {
+#pragma unroll
+                        for (int j = 0; j < OB; j += 4)
+                            *reinterpret_cast<float4 *>(Wp + rowoff + j) =
+                                make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < OB; j++)
+                            if (zl0 + j < Zc) Wp[rowoff + j] = o[j];
+                    }
+                }
+            });
         }
         {
             long long t1 = GB_B1NOW();

@@ -1,371 +1,24 @@
 // Fused SPECT forward projector (rotate -> attenuate -> depth-dependent PSF -> ray sum)
-// and the cross-chunk reduction with its likelihood-ratio epilogue.
+// and the cross-chunk reduction with its likelihood-ratio epilogue: the projector without
+// PSF, the reduction and the launchers (the PSF kernel is in spect_fwd_psf.cuh).
 //
 // Reference: SPECTSystemMatrix.forward (projectors/SPECT/spect_system_matrix.py:120-157)
-// with SPECTAttenuationTransform.forward (transforms/SPECT/attenuation.py:72-92) and
-// SPECTPSFTransform.forward -> Seperable1DBlurNet.forward (transforms/SPECT/psf.py:27-41,
-// 199-214); the ratio epilogue is PoissonLogLikelihood.compute_gradient's
-// g / (H f + s + delta) (likelihoods/poisson_log_likelihood.py:33-36).
-//
-// Work decomposition: one CTA per (angle, chunk of x planes, z slab).  The CTA sweeps
-// its planes; per plane it samples the rotated object (times A) into shared memory,
-// blurs along y into a transposed buffer, blurs along z and accumulates the ray sum
-// in registers.  Partial sums of the chunks go to a scratch buffer and are reduced
-// in a fixed order by k_reduce (deterministic results).
-#include "spect_blur.cuh"
+// with SPECTAttenuationTransform.forward (transforms/SPECT/attenuation.py:72-92); the
+// ratio epilogue is PoissonLogLikelihood.compute_gradient's g / (H f + s + delta)
+// (likelihoods/poisson_log_likelihood.py:33-36).
 #include "spect_kernels.cuh"
 #include "spect_launch.h"
 
 namespace gb {
 
-#ifdef GB_PHASE_TIMING
-// Per-CTA cycle counts of the forward kernel's phases (diagnostic builds only):
-// [0] waits for the attenuation copy, [1] phase 1, [2] phase 2, [3] phase 3,
-// [4] planes processed, [5] total, [6] rows sampled, [7] output rows x taps.
-__device__ unsigned long long g_fwd_phase_cycles[4096 * 8];
-#define GB_T(k, v)                                              \
-    do {                                                        \
-        if (threadIdx.x == 0) tacc[k] += (v);                   \
-    } while (0)
-#define GB_NOW() clock64()
-#else
-#define GB_T(k, v) \
-    do {           \
-        (void)(v); \
-    } while (0)
-#define GB_NOW() 0LL
-#endif
-
-// Does the sample segment of plane xp (rows y in [ya, yb]) touch the object square
-// [pad-1, pad+N] x [pad-1, pad+N] in padded coordinates?  Liang-Barsky clip.
-__device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, int xp, int ya,
-                                           int yb) {
-    float ixa, iya, ixb, iyb;
-    rot_coords(th, g.lin[xp], g.lin[ya], g.half, ixa, iya);
-    rot_coords(th, g.lin[xp], g.lin[yb], g.half, ixb, iyb);
-    float lo = (float)g.pad - 1.5f, hi = (float)(g.pad + g.N) + 0.5f;
-    float t0 = 0.f, t1 = 1.f;
-    float p[2] = {ixa, iya}, d[2] = {ixb - ixa, iyb - iya};
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        if (fabsf(d[k]) < 1e-12f) {
-            if (p[k] < lo || p[k] > hi) return false;
-        } else {
-            float ta = (lo - p[k]) / d[k], tb = (hi - p[k]) / d[k];
-            if (ta > tb) { float t = ta; ta = tb; tb = t; }
-            t0 = fmaxf(t0, ta);
-            t1 = fminf(t1, tb);
-        }
-    }
-    return t0 <= t1;
-}
-
-// ---------------------------------------------------------------- with PSF
-// Shared-memory layout (per CTA):
-//   S  [SR][SC]: rotated, attenuated samples; row r <-> padded y = pad - H + r,
-//                column c <-> z = z0 - HP + c  (HP = H rounded up to 4: 16-byte aligned
-//                z quads).  Before phase 1 of a plane, the attenuation rows of that
-//                plane are bulk-copied (TMA) into S and multiplied in place.
-//   Tt [TR][TS]: y-blurred plane, transposed; row c <-> z = z0 - HP + c, column = output y
-//   taps [2][2][K]: double-buffered y / z taps of the current plane
-//   one mbarrier for the TMA copies
-// Per plane only the rows the rotated object square can reach are sampled / blurred.
-// FIXED: the tile fits 128 output rows and a z slab of at most ZW (128 for 512-thread
-// CTAs, 64 for 256-thread CTAs), so the shared-memory row strides are compile-time
-// constants (immediate-offset loads in the blur loops).
-// TPB: 512 threads and one CTA per SM, or 256 threads with a half-width z slab and two
-// CTAs per SM (one CTA's gathers overlap the other's blur arithmetic).
-template <int K, bool VEC, bool FIXED, int TPB>
-__global__ void __launch_bounds__(TPB, 512 / TPB)
-    k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
-              const int4 *__restrict__ items, int Zt, float *__restrict__ partials) {
-    constexpr int H = K / 2;
-    constexpr int ZW = TPB >= 512 ? 128 : 64;
-    constexpr int HP = (H + 3) / 4 * 4;
-    constexpr int OB = (K <= 31) ? 8 : 4;  // outputs per task
-    constexpr int NACC = 32 / OB;          // phase-3 tasks per thread
-    const int4 item = items[blockIdx.x];  // (slot, first plane, end plane)
-    const int slot = item.x;
-    const int ga = alist[slot];
-    const int N = g.N, nz = g.nz;
-    const int z0 = blockIdx.y * Zt;
-    const int Zc = min(Zt, nz - z0);
-    const int N8 = (N + OB - 1) / OB * OB;
-    const int Z8 = (Zc + OB - 1) / OB * OB;
-    constexpr int SC_FIX = ZW + 2 * HP, TS_FIX = 129;
-    const int SC = FIXED ? SC_FIX : Z8 + 2 * HP, SR = N8 + 2 * H;
-    const int TS = FIXED ? TS_FIX : N8 + 1, TR = Z8 + 2 * HP;
-    extern __shared__ __align__(128) float sm[];
-    float *S = sm;
-    float *Tt = S + SR * SC;
-    float *tp = Tt + TR * TS;
-    unsigned long long *bar =
-        reinterpret_cast<unsigned long long *>(tp + ((4 * K + 1) & ~1));
-    for (int i = threadIdx.x; i < SR * SC + TR * TS; i += TPB) sm[i] = 0.f;
-
-    float th[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * ga + k];
-    const int grp = g.group[ga];
-    const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
-    const bool amul = A && g.att_first;
-    const bool use_tma = VEC && amul;
-    const int x0 = item.y, x1 = item.z;
-    const int zv_lo = max(0, z0 - H), zv_hi = min(nz, z0 + Zc + H);  // z needed by the blur
-    const int cz_lo = zv_lo - z0 + HP, cz_hi = zv_hi - z0 + HP;
-    const int ncol = cz_hi - cz_lo;
-    const int ylo = max(0, g.pad - H), yhi = min(g.Lp, g.pad + N + H);  // sampled rows
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int nwarp = TPB / 32;
-    const int zq_lo = zv_lo & ~3, zq_hi = (zv_hi + 3) & ~3;  // z quads (vector path)
-    const int nq = (zq_hi - zq_lo) >> 2;
-    const unsigned row_bytes = (unsigned)(zq_hi - zq_lo) * 4u;
-    const int qcol0 = zq_lo - z0 + HP;  // S column of the first quad
-    if (threadIdx.x == 0 && use_tma) mbar_init(bar, 1);
-    float acc[NACC][OB];
-    int ty[NACC], tz[NACC];  // phase-3 task (output row, z block) of this thread
-    // each warp owns whole z blocks and, for them, every 32-row chunk: restricting a
-    // plane's rows removes the same share of work from every warp
-    // (falls back to a linear task order when the rows need more chunks than tasks)
-    {
-        const int n_yc = (N8 + 31) >> 5;
-        const bool balanced = n_yc <= NACC;
-#pragma unroll
-        for (int k = 0; k < NACC; k++) {
-            if (balanced) {
-                ty[k] = 32 * (k % n_yc) + lane;
-                tz[k] = warp + nwarp * (k / n_yc);
-                if (ty[k] >= N8 || k / n_yc >= NACC / n_yc) tz[k] = 1 << 20;  // no task
-            } else {
-                const int task = threadIdx.x + k * TPB;
-                ty[k] = task % N8;
-                tz[k] = task / N8;
-            }
-#pragma unroll
-            for (int j = 0; j < OB; j++) acc[k][j] = 0.f;
-        }
-    }
-    __syncthreads();
-
-    bool failed = false;  // this thread's bounded wait gave up
-    unsigned failed_phase = 0;
-    // next plane with any sample on the object, from xp on; rows in [ra, rb]
-    auto next_plane = [&](int xp, int &ra, int &rb) {
-        for (; xp < x1; ++xp)
-            if (plane_rows(g, th, xp, ylo, yhi, 0.5f, ra, rb)) return xp;
-        return x1;
-    };
-    // bulk-copy the attenuation rows [ra, rb] of plane xp into S (warp 0)
-    auto issue_tma = [&](int xp, int ra, int rb) {
-        if (warp != 0 || __any_sync(0xffffffffu, failed)) return;
-        if (lane == 0) {
-            fence_proxy_async_smem();
-            mbar_arrive_expect_tx(bar, row_bytes * (unsigned)(rb - ra + 1));
-        }
-        __syncwarp();
-        const float *src = A + ((size_t)xp * g.nya + (ra - g.ya_lo)) * nz + zq_lo;
-        for (int y = ra + lane; y <= rb; y += 32)
-            tma_load_1d(S + (y - (g.pad - H)) * SC + qcol0, src + (size_t)(y - ra) * nz,
-                        row_bytes, bar);
-    };
-
-    int ra = 0, rb = -1, pra = 0, prb = -1;  // current and previous sampled rows
-    int xp = next_plane(x0, ra, rb);
-    if (use_tma && xp < x1) issue_tma(xp, ra, rb);
-    int parity = 0;
-    unsigned phase = 0;
-#ifdef GB_PHASE_TIMING
-    unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const long long t_start = clock64();
-#endif
-    long long t0 = GB_NOW();
-    while (xp < x1) {
-        t0 = GB_NOW();
-        const float lr = g.lin[xp];
-        float *tap = tp + parity * 2 * K;
-        if (threadIdx.x < K) {
-            tap[threadIdx.x] = g.taps_r[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x];
-            tap[K + threadIdx.x] =
-                g.psf2d ? g.taps_z[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x] : 0.f;
-        }
-        if (use_tma) {
-            // A thread whose bounded wait gives up flags the plan and stops waiting (its
-            // results are invalid); every thread still reaches every barrier.
-            if (!failed && !mbar_wait_bounded(bar, phase, 1u << 16)) {
-                failed = true;
-                failed_phase = phase;
-                if (g.err) atomicExch(g.err, GB_ERR_WAIT_TIMEOUT);
-            }
-            phase ^= 1u;
-        }
-        {
-            long long t1 = GB_NOW();
-            GB_T(0, t1 - t0);
-            t0 = t1;
-        }
-        // phase 1: rotated samples of rows [ra, rb] (times A when attenuation precedes
-        // the PSF); stale rows of the previous plane are cleared
-        const float *Ap = A ? A + (size_t)xp * g.nya * nz : nullptr;
-        if (VEC) {
-            for (int y = pra + warp; y <= prb; y += nwarp) {
-                if (y >= ra && y <= rb) continue;
-                float *Sr = S + (y - (g.pad - H)) * SC + qcol0;
-                for (int q = lane; q < nq; q += 32)
-                    *reinterpret_cast<float4 *>(Sr + 4 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-            // four consecutive rows per warp and batch: neighbouring rows share about half
-            // of their bilinear taps, which then hit in L1
-            for (int y0 = ra + 4 * warp; y0 <= rb; y0 += 4 * nwarp) {
-                int ys[4];
-                bool okr[4];
-                Bilin b[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    ys[u] = y0 + u;
-                    okr[u] = ys[u] <= rb;
-                    float ix, iy;
-                    rot_coords(th, lr, g.lin[okr[u] ? ys[u] : y0], g.half, ix, iy);
-                    b[u] = bilin(ix, iy);
-                }
-                for (int q = lane; q < nq; q += 32) {
-                    const int z = zq_lo + 4 * q;
-                    float4 v[4];
-                    bool h[4];
-#pragma unroll
-                    for (int u = 0; u < 4; u++)
-                        h[u] = okr[u] && sample4(f, N, N, nz, g.pad, g.pad, b[u], z, v[u]);
-#pragma unroll
-                    for (int u = 0; u < 4; u++) {
-                        if (!okr[u]) continue;
-                        float4 *dst = reinterpret_cast<float4 *>(
-                            S + (ys[u] - (g.pad - H)) * SC + qcol0 + 4 * q);
-                        float4 o = v[u];
-                        if (amul) {
-                            float4 a = use_tma ? *dst
-                                               : (h[u] ? __ldg(reinterpret_cast<const float4 *>(
-                                                             Ap + (size_t)(ys[u] - g.ya_lo) * nz + z))
-                                                       : make_float4(0.f, 0.f, 0.f, 0.f));
-                            o = mul4(o, a);
-                        }
-                        *dst = h[u] ? o : make_float4(0.f, 0.f, 0.f, 0.f);
-                    }
-                }
-            }
-        } else {
-            for (int i = threadIdx.x; i < (yhi - ylo) * ncol; i += TPB) {
-                int y = ylo + i / ncol, c = cz_lo + i % ncol;
-                int z = z0 - HP + c;
-                float v = 0.f;
-                if (y >= ra && y <= rb) {
-                    float ix, iy;
-                    rot_coords(th, lr, g.lin[y], g.half, ix, iy);
-                    Bilin bb = bilin(ix, iy);
-                    v = sample(f, N, N, nz, g.pad, g.pad, bb, z);
-                    if (amul && v != 0.f) v = __fmul_rn(v, Ap[(size_t)(y - g.ya_lo) * nz + z]);
-                }
-                S[(y - (g.pad - H)) * SC + c] = v;
-            }
-        }
-        __syncthreads();
-        {
-            long long t1 = GB_NOW();
-            GB_T(1, t1 - t0);
-            t0 = t1;
-        }
-        // output rows (local y in [0, N)) that the blurred plane can reach
-        const int o_lo = max(0, ra - H - g.pad), o_hi = min(N, rb + H - g.pad + 1);
-        const int b_lo = o_lo / OB, b_hi = (o_hi + OB - 1) / OB;
-        // phase 2: blur along y, write transposed (tap tier of the plane)
-        constexpr int KK0 = 2 * tier_half(K, 0) + 1, KK1 = 2 * tier_half(K, 1) + 1;
-        int tier = 2;
-        if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : 2;
-        if (tier == 0)
-            blur_first<K, KK0, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
-        else if (tier == 1)
-            blur_first<K, KK1, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
-        else
-            blur_first<K, K, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
-        GB_T(6, rb - ra + 1);
-        GB_T(7, (b_hi - b_lo) * OB * (tier == 0 ? KK0 : (tier == 1 ? KK1 : K)));
-        __syncthreads();
-        {
-            long long t1 = GB_NOW();
-            GB_T(2, t1 - t0);
-            t0 = t1;
-        }
-        // S is free until the next phase 1: start the next plane's attenuation copy
-        pra = ra;
-        prb = rb;
-        int nra = 0, nrb = -1;
-        const int nxp = next_plane(xp + 1, nra, nrb);
-        if (use_tma && nxp < x1) issue_tma(nxp, nra, nrb);
-        // phase 3: blur along z (2D PSF), optional attenuation after the PSF, accumulate
-        {
-            const int y_lo = b_lo * OB, y_hi = b_hi * OB;
-#define GB_FWD_PHASE3(KK)                                                                   \
-    {                                                                                       \
-        float w[KK];                                                                        \
-        load_taps<K, KK>(tap + K, w);                                                       \
-        _Pragma("unroll") for (int k = 0; k < NACC; k++) {                                  \
-            const int y = ty[k], zb = tz[k];                                                \
-            if (zb * OB < Z8 && y >= y_lo && y < y_hi) {                                    \
-                float o[OB];                                                                \
-                if (g.psf2d) {                                                              \
-                    blur_second<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, o);              \
-                } else {                                                                    \
-                    _Pragma("unroll") for (int j = 0; j < OB; j++) o[j] =                   \
-                        Tt[(zb * OB + j + HP) * TS + y];                                    \
-                }                                                                           \
-                if (Ap && !g.att_first && y < N) {                                          \
-                    _Pragma("unroll") for (int j = 0; j < OB; j++) {                        \
-                        int z = z0 + zb * OB + j;                                           \
-                        if (z < nz)                                                         \
-                            o[j] = __fmul_rn(o[j], Ap[(size_t)(g.pad + y - g.ya_lo) * nz + z]); \
-                    }                                                                       \
-                }                                                                           \
-                _Pragma("unroll") for (int j = 0; j < OB; j++) acc[k][j] += o[j];           \
-            }                                                                               \
-        }                                                                                   \
-    }
-            if (tier == 0)
-                GB_FWD_PHASE3(KK0)
-            else if (tier == 1)
-                GB_FWD_PHASE3(KK1)
-            else
-                GB_FWD_PHASE3(K)
-#undef GB_FWD_PHASE3
-        }
-        {
-            long long t1 = GB_NOW();
-            GB_T(3, t1 - t0);
-            GB_T(4, 1);
-        }
-        parity ^= 1;
-        xp = nxp;
-        ra = nra;
-        rb = nrb;
-    }
-    if (failed) mbar_wait_bounded(bar, failed_phase, 1u << 16);
-#ifdef GB_PHASE_TIMING
-    if (threadIdx.x == 0 && blockIdx.x < 4096) {
-        tacc[5] = clock64() - t_start;
-        for (int k = 0; k < 8; k++) g_fwd_phase_cycles[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
-    }
-#endif
-    // partial ray sums of this item
-    float *out = partials + (size_t)blockIdx.x * N * nz;
-#pragma unroll
-    for (int k = 0; k < NACC; k++) {
-        const int y = ty[k], zb = tz[k];
-        if (zb * OB < Z8 && y < N) {
-#pragma unroll
-            for (int j = 0; j < OB; j++) {
-                int z = z0 + zb * OB + j;
-                if (z - z0 < Zc) out[(size_t)y * nz + z] = acc[k][j];
-            }
-        }
-    }
-}
+// per-bucket PSF forward entry points (spect_fwd_k*.cu)
+#define GB_DECL_FWD(KK)                                                                      \
+    cudaError_t launch_fwd_psf_##KK(const SpectDev &g, const float *f, const int *alist,     \
+                                    const int4 *items, int n_items, int Zt, int tpb,         \
+                                    float *partials, cudaStream_t st);                      \
+    cudaError_t setup_fwd_##KK(size_t smem, int tpb);
+GB_FOR_EACH_K(GB_DECL_FWD)
+#undef GB_DECL_FWD
 
 // ------------------------------------------------------------- without PSF
 // One thread per output (y, z) of an item's planes; A read on the fly.
@@ -422,7 +75,7 @@ __global__ void k_reduce(const int *__restrict__ ioff, int NZ, const float *__re
 }
 
 // ------------------------------------------------------------- launchers
-static bool fwd_fixed(int K, int N, int Zt, int tpb) {
+static bool fwd_fixed_host(int K, int N, int Zt, int tpb) {
     int OB = (K <= 31) ? 8 : 4;
     return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= (tpb >= 512 ? 128 : 64);
 }
@@ -431,7 +84,7 @@ size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb) {
     int H = K / 2, HP = (H + 3) / 4 * 4, OB = (K <= 31) ? 8 : 4;
     int N8 = (N + OB - 1) / OB * OB;
     int Z8 = (Zt + OB - 1) / OB * OB;
-    const bool fx = fwd_fixed(K, N, Zt, tpb);
+    const bool fx = fwd_fixed_host(K, N, Zt, tpb);
     const int ZW = tpb >= 512 ? 128 : 64;
     size_t SC = fx ? ZW + 2 * HP : Z8 + 2 * HP, TS = fx ? 129 : N8 + 1;
     return sizeof(float) * ((size_t)(N8 + 2 * H) * SC + (size_t)(Z8 + 2 * HP) * TS +
@@ -439,47 +92,11 @@ size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb) {
            sizeof(unsigned long long);
 }
 
-template <int K, int TPB>
-static cudaError_t launch_fwd_psf_t(const SpectDev &g, const float *f, const int *alist,
-                                    const int4 *items, int n_items, int Zt, float *partials,
-                                    cudaStream_t st) {
-    size_t smem = fwd_psf_smem_bytes(K, g.N, Zt, TPB);
-    dim3 grid(n_items, (g.nz + Zt - 1) / Zt);
-    const bool fx = fwd_fixed(K, g.N, Zt, TPB);
-    if (g.nz % 4 == 0) {
-        if (fx)
-            k_fwd_psf<K, true, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
-        else
-            k_fwd_psf<K, true, false, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
-    } else {
-        if (fx)
-            k_fwd_psf<K, false, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
-        else
-            k_fwd_psf<K, false, false, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt,
-                                                                    partials);
-    }
-    return cudaGetLastError();
-}
-
-template <int K, int TPB>
-static cudaError_t setup_fwd_t(size_t smem) {
-    const void *fns[4] = {(const void *)k_fwd_psf<K, true, true, TPB>,
-                          (const void *)k_fwd_psf<K, true, false, TPB>,
-                          (const void *)k_fwd_psf<K, false, true, TPB>,
-                          (const void *)k_fwd_psf<K, false, false, TPB>};
-    for (const void *fn : fns) {
-        cudaError_t e =
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-}
-
 cudaError_t setup_fwd(int K, size_t smem, int tpb) {
     switch (K) {
 #define GB_SETUP_CASE(KK) \
     case KK:              \
-        return tpb >= 512 ? setup_fwd_t<KK, 512>(smem) : setup_fwd_t<KK, 256>(smem);
+        return setup_fwd_##KK(smem, tpb);
         GB_FOR_EACH_K(GB_SETUP_CASE)
 #undef GB_SETUP_CASE
         default:
@@ -495,11 +112,9 @@ cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, cons
         return cudaGetLastError();
     }
     switch (g.K) {
-#define GB_FWD_CASE(KK)                                                                      \
-    case KK:                                                                                 \
-        return tpb >= 512                                                                    \
-                   ? launch_fwd_psf_t<KK, 512>(g, f, alist, items, n_items, Zt, partials, st) \
-                   : launch_fwd_psf_t<KK, 256>(g, f, alist, items, n_items, Zt, partials, st);
+#define GB_FWD_CASE(KK) \
+    case KK:            \
+        return launch_fwd_psf_##KK(g, f, alist, items, n_items, Zt, tpb, partials, st);
         GB_FOR_EACH_K(GB_FWD_CASE)
 #undef GB_FWD_CASE
         default:
@@ -507,16 +122,6 @@ cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, cons
     }
 }
 
-#ifdef GB_PHASE_TIMING
-extern "C" int gb_debug_fwd_phase_cycles(unsigned long long *out, int n) {
-    return (int)cudaMemcpyFromSymbol(out, g_fwd_phase_cycles,
-                                     sizeof(unsigned long long) * (size_t)n);
-}
-extern "C" int gb_debug_phase_reset(void) {
-    static unsigned long long zero[4096 * 8];
-    return (int)cudaMemcpyToSymbol(g_fwd_phase_cycles, zero, sizeof(zero));
-}
-#endif
 
 cudaError_t launch_reduce(int n_slots, const int *ioff, int NZ, const float *partials, float *out,
                           int ratio, const float *gproj, const float *sadd, const int *alist,

@@ -1,0 +1,8 @@
+// PSF forward projector instance for the 45-tap bucket (spect_fwd_psf.cuh).
+#include "spect_fwd_psf.cuh"
+
+namespace gb {
+
+GB_FWD_PSF_INSTANCE(45)
+
+}  // namespace gb

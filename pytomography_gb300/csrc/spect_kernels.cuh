@@ -41,6 +41,7 @@ struct SpectDev {
     int att_first;          // forward order: attenuation before PSF ("ap")
     int psf;                // PSF present
     int psf2d;              // PSF blurs z as well
+    unsigned long long *phase;  // diagnostic builds: per-CTA forward phase cycles, or null
 };
 
 // Epilogue of the gather back-projector.

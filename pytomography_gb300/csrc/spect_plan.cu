@@ -97,6 +97,7 @@ static void free_plan(gb_spect_plan *p) {
     cudaFree(p->d_lin); cudaFree(p->d_theta_fwd); cudaFree(p->d_theta_bwd);
     cudaFree(p->d_taps_r); cudaFree(p->d_taps_z); cudaFree(p->d_A); cudaFree(p->d_group);
     cudaFree(p->d_tier);
+    cudaFree(p->dev.phase);
     cudaFree(p->d_alist); cudaFree(p->d_items); cudaFree(p->d_ioff);
     cudaFree(p->d_partials); cudaFree(p->d_W); cudaFree(p->d_ratio);
     cudaFree(p->d_bp);
@@ -155,8 +156,8 @@ static std::vector<double> plane_work(const gb_spect_plan *p, int a, bool fwd) {
     for (int xp = 0; xp < p->Lp; xp++) {
         int ra, rb;
         if (!host_plane_rows(p, a, xp, ylo, yhi, fwd ? 0.5 : 1.5, ra, rb)) continue;
-        const int tier = p->h_tier.empty() ? 2 : p->h_tier[(size_t)grp * p->Lp + xp];
-        const double kk = 2 * tier_half(K, tier) + 1;
+        const int tier = p->h_tier.empty() ? kTiers - 1 : p->h_tier[(size_t)grp * p->Lp + xp];
+        const double kk = tier_taps(K, tier);
         const double rows = rb - ra + 1;
         if (fwd) {
             const int o = std::min(p->N, rb + H - p->pad + 1) - std::max(0, ra - H - p->pad);
@@ -479,7 +480,7 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
                 }
             }
         // tap tier of every plane: the narrowest unrolled loop that holds its nonzero taps
-        std::vector<signed char> tier((size_t)ng * Lp, 2);
+        std::vector<signed char> tier((size_t)ng * Lp, kTiers - 1);
         const int Hk = K / 2;
         for (int gi = 0; gi < ng; gi++)
             for (int x = 0; x < Lp; x++) {
@@ -489,8 +490,9 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
                     for (int t = 0; t < K; t++)
                         if (tab[((size_t)gi * Lp + x) * K + t] != 0.f) h = std::max(h, std::abs(t - Hk));
                 }
-                tier[(size_t)gi * Lp + x] =
-                    h <= tier_half(K, 0) ? 0 : (h <= tier_half(K, 1) ? 1 : 2);
+                int t = 0;
+                while (t < kTiers - 1 && h > tier_half(K, t)) t++;
+                tier[(size_t)gi * Lp + x] = (signed char)t;
             }
         p->h_tier = tier;
         FAIL_CUDA(cudaMalloc(&p->d_tier, tier.size()));
@@ -891,6 +893,23 @@ gb_status gb_rdp_gradient(const float *f, float *grad, int32_t nx, int32_t ny, i
     GB_CUDA(launch_rdp(f, grad, nx, ny, nz, u, beta_scale, as_stream(stream)));
     return GB_OK;
 }
+
+#ifdef GB_PHASE_TIMING
+// Diagnostic builds: per-CTA phase cycle counts of the plan's forward launches ([4096][8],
+// layout in spect_fwd_psf.cuh), attached on first use.
+extern "C" int gb_debug_fwd_phase_cycles(gb_spect_plan *p, unsigned long long *out, int n) {
+    if (!p->dev.phase) return -1;
+    return (int)cudaMemcpy(out, p->dev.phase, sizeof(unsigned long long) * (size_t)n,
+                           cudaMemcpyDeviceToHost);
+}
+extern "C" int gb_debug_fwd_phase_reset(gb_spect_plan *p) {
+    if (!p->dev.phase) {
+        cudaError_t e = cudaMalloc(&p->dev.phase, sizeof(unsigned long long) * 4096 * 8);
+        if (e != cudaSuccess) return (int)e;
+    }
+    return (int)cudaMemset(p->dev.phase, 0, sizeof(unsigned long long) * 4096 * 8);
+}
+#endif
 
 gb_status gb_rdp_hessian_vector(const float *f, const float *x, float *out, int32_t nx,
                                 int32_t ny, int32_t nz, float dx, float dy, float dz,
