@@ -66,6 +66,9 @@ typedef struct gb_spect_desc {
     const float *psf_taps_z;  /* host [n_groups][n_pad][psf_k]: z-direction taps per plane */
     float psf_trunc_rel;      /* taps below this fraction of a plane's largest tap are
                                  dropped (0 keeps every tap) */
+    int32_t no_pad;           /* 1: rotate in the unpadded nx x nx frame (n_pad = nx), as the
+                                 StarGuide system matrix does (transforms configured with
+                                 assume_padded=False); 0: the padded frame of SPECTSystemMatrix */
 } gb_spect_desc;
 
 /* Create / destroy a plan.  Creation uploads the geometry tables and precomputes the
@@ -84,6 +87,12 @@ gb_status gb_spect_device_status(gb_spect_plan *plan, int32_t *code);
 /* Interleaved angle subsets indices[i::n_subsets]
  * (spect_system_matrix.py:58-71).  n_subsets >= 1. */
 gb_status gb_spect_set_subsets(gb_spect_plan *plan, int32_t n_subsets);
+/* Explicit subsets: subset s holds the counts[s] angle indices that follow those of the
+ * earlier subsets in angle_idx (host arrays), in projection-row order.  Replaces the
+ * interleaved subsets until gb_spect_set_subsets is called again; used for the StarGuide
+ * subsets of whole angle groups (starguide_system_matrix.py:166-179). */
+gb_status gb_spect_set_subset_lists(gb_spect_plan *plan, int32_t n_subsets,
+                                    const int32_t *angle_idx, const int32_t *counts);
 /* Number of angles in a subset (-1 = all angles). */
 int32_t gb_spect_subset_size(const gb_spect_plan *plan, int32_t subset);
 
@@ -286,6 +295,22 @@ gb_status gb_pet_lm_to_sino(const int32_t *events, int64_t n_events, int32_t nco
                             int32_t n_rings, int32_t n_angles, int32_t n_radial,
                             int32_t n_planes, int32_t tof_num_bins, int32_t normalization,
                             float *sino, gb_stream_t stream);
+
+/* --------------------------------------------------------- StarGuide window */
+/* Detector window of the StarGuide system matrix (projectors/SPECT/
+ * starguide_system_matrix.py:30-110) applied to projections of a no_pad plan (all device):
+ * out [n][width][nz] = scale[i] * full[i] translated along y by shift[i] pixels (output
+ * column y reads input column y - shift, linear interpolation, zero outside) on the
+ * columns int(ny/2) - width/2 ... + width - 1.  The reference uses width 16, shift =
+ * offset / dx and scale = time / 1000. */
+gb_status gb_starguide_window(const float *full, float *out, int32_t n, int32_t ny, int32_t nz,
+                              int32_t width, const float *shift, const float *scale,
+                              gb_stream_t stream);
+/* The back-projection side: full [n][ny][nz] = the window of scale[i] * proj[i]
+ * zero-padded to ny columns ((ny - width) even), translated by -shift[i]. */
+gb_status gb_starguide_window_adjoint(const float *proj, float *full, int32_t n, int32_t ny,
+                                      int32_t nz, int32_t width, const float *shift,
+                                      const float *scale, gb_stream_t stream);
 
 /* ---------------------------------------------------- object-space operators */
 /* Separable Gaussian filter, GaussianFilter.forward (transforms/shared/filters.py:47-63):

@@ -30,6 +30,7 @@ class SpectDesc(ctypes.Structure):
         ("psf_2d", c_int), ("psf_n_groups", c_int), ("psf_group", c_void_p),
         ("psf_k", c_int), ("psf_taps_r", c_void_p), ("psf_taps_z", c_void_p),
         ("psf_trunc_rel", c_float),
+        ("no_pad", c_int),
     ]
 
 
@@ -81,6 +82,11 @@ SIGNATURES = [
     ("gb_spect_set_subsets", c_int, [c_void_p, c_int]),
     ("gb_spect_device_status", c_int, [c_void_p, ctypes.POINTER(c_int)]),
     ("gb_spect_subset_size", c_int, [c_void_p, c_int]),
+    ("gb_spect_set_subset_lists", c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    ("gb_starguide_window", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p,
+                                    c_void_p, c_void_p]),
+    ("gb_starguide_window_adjoint", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                            c_void_p, c_void_p, c_void_p]),
     ("gb_spect_get_tuning", c_int, [c_void_p, ctypes.POINTER(SpectTuning)]),
     ("gb_spect_set_tuning", c_int, [c_void_p, ctypes.POINTER(SpectTuning)]),
     ("gb_spect_autotune", c_int, [c_void_p, c_int, c_int, ctypes.POINTER(SpectTuning), c_void_p]),

@@ -71,6 +71,7 @@ struct gb_spect_plan {
     int4 *d_items = nullptr;
     int *d_ioff = nullptr;
     int n_subsets = 0;
+    std::vector<std::vector<int>> explicit_subsets;  // caller's subset lists, if set
     struct List {
         int alist_off = 0, n = 0;
         int fitem_off = 0, n_fitems = 0;  // forward items in d_items
@@ -244,10 +245,15 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
         for (int a = 0; a < p->n_angles; a++) l.push_back(a);
         angle_lists.push_back(l);
     }
-    for (int s = 0; s < n_subsets; s++) {
-        std::vector<int> l;
-        for (int a = s; a < p->n_angles; a += n_subsets) l.push_back(a);
-        angle_lists.push_back(l);
+    if (!p->explicit_subsets.empty()) {
+        n_subsets = (int)p->explicit_subsets.size();
+        for (const auto &l : p->explicit_subsets) angle_lists.push_back(l);
+    } else {
+        for (int s = 0; s < n_subsets; s++) {
+            std::vector<int> l;
+            for (int a = s; a < p->n_angles; a += n_subsets) l.push_back(a);
+            angle_lists.push_back(l);
+        }
     }
     const bool psf = p->dev.psf;
     const int zs_f = psf ? (p->nz + p->Zt_fwd - 1) / p->Zt_fwd : 1;
@@ -389,7 +395,7 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     auto *p = new gb_spect_plan();
     p->N = d->nx;
     p->nz = d->nz;
-    p->pad = (int)std::ceil((std::sqrt(2.0) * d->nx - d->nx) / 2.0);
+    p->pad = d->no_pad ? 0 : (int)std::ceil((std::sqrt(2.0) * d->nx - d->nx) / 2.0);
     p->Lp = p->N + 2 * p->pad;
     p->n_angles = d->n_angles;
     p->dx = d->dx; p->dy = d->dy; p->dz = d->dz;
@@ -570,6 +576,28 @@ gb_status gb_spect_set_subsets(gb_spect_plan *p, int32_t n_subsets) {
     GB_CHECK_ARG(p, "null plan");
     GB_CHECK_ARG(n_subsets >= 1 && n_subsets <= p->n_angles, "n_subsets must be in [1, %d]",
                  p->n_angles);
+    p->explicit_subsets.clear();
+    return upload_lists(p, n_subsets);
+}
+
+gb_status gb_spect_set_subset_lists(gb_spect_plan *p, int32_t n_subsets, const int32_t *angle_idx,
+                                    const int32_t *counts) {
+    clear_error();
+    GB_CHECK_ARG(p && angle_idx && counts, "null argument");
+    GB_CHECK_ARG(n_subsets >= 1, "n_subsets must be positive");
+    std::vector<std::vector<int>> lists(n_subsets);
+    long long off = 0;
+    for (int s = 0; s < n_subsets; s++) {
+        GB_CHECK_ARG(counts[s] >= 1, "subset %d is empty", s);
+        for (int k = 0; k < counts[s]; k++) {
+            const int a = angle_idx[off + k];
+            GB_CHECK_ARG(a >= 0 && a < p->n_angles, "angle index %d outside [0, %d)", a,
+                         p->n_angles);
+            lists[s].push_back(a);
+        }
+        off += counts[s];
+    }
+    p->explicit_subsets = lists;
     return upload_lists(p, n_subsets);
 }
 

@@ -44,6 +44,22 @@ class SPECTProjMeta(ProjMeta):
                              int(self.shape[2]))
 
 
+class StarGuideProjMeta(ProjMeta):
+    """StarGuide projection metadata (metadata/SPECT/starguide_metadata.py:5-34):
+    projection shape (n, window width, nz); per projection its angle (degrees),
+    acquisition time (ms), offset of the detector along y (cm) and radius (cm, for the
+    PSF)."""
+
+    def __init__(self, projection_shape: Sequence, angles: Sequence, times=None, offsets=None,
+                 radii: Sequence | None = None) -> None:
+        self.angles = angles
+        self.radii = radii
+        self.offsets = offsets
+        self.times = times
+        self.num_projections = len(angles)
+        self.shape = projection_shape
+
+
 class SPECTPSFMeta:
     """Depth-dependent PSF: sigma(d) = sigma_fit(d, *params) (cm)."""
 

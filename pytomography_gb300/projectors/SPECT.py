@@ -40,13 +40,15 @@ class SPECTSystemMatrix(SystemMatrix):
 
     def __init__(self, obj2obj_transforms, proj2proj_transforms, object_meta, proj_meta,
                  object_initial_based_on_camera_path: bool = False,
-                 psf_trunc_rel: float = 1e-7, autotune: bool = False) -> None:
+                 psf_trunc_rel: float = 1e-7, autotune: bool = False,
+                 _no_pad: bool = False) -> None:
         if proj2proj_transforms:
             raise NotImplementedError("proj2proj transforms are not part of the fused path")
         super().__init__(object_meta, proj_meta, obj2obj_transforms, proj2proj_transforms)
         self.object_initial_based_on_camera_path = object_initial_based_on_camera_path
         self.psf_trunc_rel = float(psf_trunc_rel)
         self.autotune_enabled = bool(autotune)
+        self._no_pad = bool(_no_pad)  # unpadded rotation frame (the StarGuide projector)
         self._plan = None
         self._lib = _lib.load()
         self._build_plan()
@@ -65,7 +67,12 @@ class SPECTSystemMatrix(SystemMatrix):
             raise RuntimeError("SPECTSystemMatrix needs a CUDA device (no CPU path)")
         self.device = torch.device("cuda", torch.cuda.current_device())
         n = pm.num_projections
-        Lp = om.padded_shape[0]
+        Lp = nx if self._no_pad else om.padded_shape[0]
+        for t in self.obj2obj_transforms:
+            if getattr(t, "assume_padded", True) == self._no_pad:
+                raise NotImplementedError(
+                    "transforms must be configured for the system matrix's frame "
+                    "(assume_padded=True for SPECTSystemMatrix, False for StarGuide)")
         angles = pm.angles.to(torch.float32).cpu()
         # forward rotation: RotationTransform.backward(obj, 270 - beta) -> rotate(beta - 270)
         self._theta_fwd = geometry.rotation_theta(-(270 - angles), Lp)
@@ -135,6 +142,7 @@ class SPECTSystemMatrix(SystemMatrix):
             self._psf_k = k
         else:
             self._psf_k = 1
+        desc.no_pad = 1 if self._no_pad else 0
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             torch.cuda.synchronize()
@@ -321,3 +329,111 @@ class SPECTSystemMatrix(SystemMatrix):
                                             align_corners=True)
         r = r.squeeze(0).permute(1, 2, 0)
         return r[pad:-pad, pad:-pad, :]
+
+
+class StarGuideSystemMatrix(SystemMatrix):
+    """StarGuide SPECT system matrix (projectors/SPECT/starguide_system_matrix.py:12-230).
+
+    Every projection is one detector at an angle, with a radius (PSF), an offset along y
+    and an acquisition time.  Its forward projection is the rotate -> attenuate -> PSF ->
+    sum projection of the object in the unpadded frame (transforms configured with
+    ``assume_padded=False``), translated along y by offset / dx, cropped to the detector
+    window and scaled by time / 1000.  Here the projection runs on the fused SPECT kernels
+    (one plan entry per detector, no padding) and the window on ``gb_starguide_window``;
+    the back projection pads, translates back and runs the reference back-projector.
+    Subsets are whole angle groups: subset k holds the detectors of the sorted unique
+    angles k, k + n, ... (:166-179).
+    """
+
+    def __init__(self, object_meta, proj_meta, obj2obj_transforms=None,
+                 proj2proj_transforms=None) -> None:
+        from ..metadata.SPECT import SPECTProjMeta
+        if proj2proj_transforms:
+            raise NotImplementedError("proj2proj transforms are not part of the fused path")
+        self.object_meta = object_meta
+        self.proj_meta = proj_meta
+        self.obj2obj_transforms = list(obj2obj_transforms or [])
+        self.proj2proj_transforms = []
+        n = int(proj_meta.num_projections)
+        nx, ny, nz = (int(v) for v in object_meta.shape)
+        angles = torch.as_tensor(proj_meta.angles, dtype=torch.float32).cpu()
+        radii = [0.0] * n if proj_meta.radii is None else [float(r) for r in proj_meta.radii]
+        inner = SPECTProjMeta((ny, nz), list(object_meta.dr[:2]), angles.tolist(), radii=radii)
+        self._H = SPECTSystemMatrix(self.obj2obj_transforms, [], object_meta, inner, _no_pad=True)
+        self.device = self._H.device
+        self._lib = self._H._lib
+        self.times = torch.as_tensor(proj_meta.times, dtype=torch.float32).reshape(-1, 1, 1) / 1e3
+        offsets = torch.as_tensor(proj_meta.offsets, dtype=torch.float32)
+        self._shift = (offsets / float(object_meta.dx)).to(self.device).contiguous()
+        self._scale = self.times.reshape(-1).to(self.device).contiguous()
+        self._width = int(proj_meta.shape[1])
+        self.subset_indices_array = None
+        self.n_subsets = 1
+
+    # ------------------------------------------------------------ subsets
+    def set_n_subsets(self, n_subsets: int) -> None:
+        angles = torch.as_tensor(self.proj_meta.angles)
+        groups = [torch.where(angles == a)[0] for a in torch.unique(angles)]
+        lists = [torch.cat(groups[i::n_subsets]) for i in range(n_subsets)]
+        self.subset_indices_array = [ix.to(self.device) for ix in lists]
+        self.n_subsets = n_subsets
+        flat = torch.cat(lists).to(torch.int32).numpy()
+        counts = np.array([len(ix) for ix in lists], np.int32)
+        _lib.check(self._lib.gb_spect_set_subset_lists(
+            self._H._plan, int(n_subsets), flat.ctypes.data_as(ctypes.c_void_p),
+            counts.ctypes.data_as(ctypes.c_void_p)))
+        self._H.subset_indices_array = self.subset_indices_array
+        self._H.n_subsets = n_subsets
+
+    def get_projection_subset(self, projections, subset_idx):
+        return projections[..., self.subset_indices_array[subset_idx], :, :]
+
+    def get_weighting_subset(self, subset_idx):
+        if subset_idx is None:
+            return 1
+        return len(self.subset_indices_array[subset_idx]) / self.proj_meta.num_projections
+
+    def _rows(self, subset_idx):
+        if subset_idx is None:
+            return torch.arange(self.proj_meta.num_projections, device=self.device)
+        return self.subset_indices_array[subset_idx]
+
+    # ------------------------------------------------------------ projectors
+    def forward(self, object, subset_idx=None):
+        full = self._H.forward(object, subset_idx)
+        rows = self._rows(subset_idx)
+        shift = self._shift[rows].contiguous()
+        scale = self._scale[rows].contiguous()
+        n, ny, nz = full.shape
+        out = torch.empty((n, self._width, nz), device=self.device)
+        _lib.check(self._lib.gb_starguide_window(_lib.ptr(full), _lib.ptr(out), n, ny, nz,
+                                                 self._width, _lib.ptr(shift), _lib.ptr(scale),
+                                                 _lib.stream_handle(self.device)))
+        return out
+
+    def backward(self, proj, subset_idx=None):
+        p = proj.to(self.device, torch.float32).contiguous()
+        rows = self._rows(subset_idx)
+        shift = self._shift[rows].contiguous()
+        scale = self._scale[rows].contiguous()
+        n, _, nz = p.shape
+        ny = int(self.object_meta.shape[1])
+        full = torch.empty((n, ny, nz), device=self.device)
+        _lib.check(self._lib.gb_starguide_window_adjoint(_lib.ptr(p), _lib.ptr(full), n, ny, nz,
+                                                         self._width, _lib.ptr(shift),
+                                                         _lib.ptr(scale),
+                                                         _lib.stream_handle(self.device)))
+        return self._H.backward(full, subset_idx)
+
+    def compute_normalization_factor(self, subset_idx=None):
+        ones = torch.ones(tuple(self.proj_meta.shape), device=self.device)
+        if subset_idx is not None:
+            ones = self.get_projection_subset(ones, subset_idx)
+        return self.backward(ones, subset_idx)
+
+    def _get_object_initial(self, device=None):
+        return torch.ones(tuple(self.object_meta.shape), device=self.device if device is None
+                          else device)
+
+    def _get_prior_FOV_scale(self):
+        return torch.ones(tuple(self.object_meta.shape), device=self.device)

@@ -28,8 +28,8 @@ class SPECTAttenuationTransform(Transform):
                                       "pass attenuation_map")
         if attenuation_map is None:
             raise Exception("Please supply only one of `attenuation_map` or `filepath` as arguments")
-        if not assume_padded:
-            raise NotImplementedError("inside SPECTSystemMatrix objects are always padded")
+        # assume_padded=False: the attenuation map is rotated in the unpadded frame, as the
+        # StarGuide system matrix needs (attenuation.py:85-89)
         self.attenuation_map = attenuation_map
         self.mode = mode
         self.assume_padded = assume_padded
@@ -49,8 +49,6 @@ class SPECTPSFTransform(Transform):
         if psf_operator is not None:
             raise NotImplementedError("a user psf_operator network cannot be fused; "
                                       "use psf_meta")
-        if not assume_padded:
-            raise NotImplementedError("inside SPECTSystemMatrix objects are always padded")
         self.psf_meta = psf_meta
         self.psf_operator = None
         self.assume_padded = assume_padded
@@ -60,7 +58,11 @@ class SPECTPSFTransform(Transform):
         self._configure_tables()
 
     def _get_sigma(self, radius: float) -> np.ndarray:
-        dim = self.object_meta.shape[0] + 2 * geometry.compute_pad_size(self.object_meta.shape[0])
+        """Per-plane sigma over the padded x extent, or the unpadded one with
+        assume_padded=False (psf.py:172-197)."""
+        dim = self.object_meta.shape[0]
+        if self.assume_padded:
+            dim += 2 * geometry.compute_pad_size(self.object_meta.shape[0])
         return geometry.psf_sigma(dim, radius, self.object_meta.dx, self.psf_meta)
 
     def _compute_kernel_size(self, radius, axis) -> int:

@@ -361,6 +361,49 @@ def multibed_case(out):
     print("wrote multibed", rec["stitched"].shape)
 
 
+def starguide_case(out):
+    """StarGuideSystemMatrix (projectors/SPECT/starguide_system_matrix.py:12-230) with
+    StarGuideProjMeta (metadata/SPECT/starguide_metadata.py): 12 detectors at 3 angles with
+    per-detector offsets, radii and times; attenuation and PSF on the unpadded frame
+    (assume_padded=False, which this path needs)."""
+    from pytomography.metadata.SPECT import StarGuideProjMeta
+    from pytomography.projectors.SPECT import StarGuideSystemMatrix
+    set_precision(torch.float32)
+    shape, dr = (32, 32, 8), (0.5, 0.5, 0.5)
+    rng = np.random.default_rng(81)
+    angles = np.array([10.0, 100.0, 215.0] * 4)
+    offsets = rng.uniform(-3.0, 3.0, 12)
+    radii = rng.uniform(15.0, 25.0, 12)
+    times = rng.uniform(500.0, 1500.0, 12)
+    f_true, mu_np = ellipsoid_phantom(shape, dr, 82, n_ell=2)
+    om = SPECTObjectMeta(list(dr), shape)
+    rec = {"shape": np.array(shape), "dr": np.array(dr), "angles": angles, "offsets": offsets,
+           "radii": radii, "times": times, "object": f_true, "mu": mu_np}
+    g = torch.Generator().manual_seed(83)
+    proj = torch.rand((12, 16, shape[2]), generator=g)
+    rec["proj"] = proj.numpy()
+    for name, with_psf in (("att", False), ("att_psf", True)):
+        pm = StarGuideProjMeta((12, 16, shape[2]), torch.tensor(angles, dtype=torch.float32),
+                               times=torch.tensor(times, dtype=torch.float32),
+                               offsets=torch.tensor(offsets, dtype=torch.float32),
+                               radii=[float(r) for r in radii])
+        ts = [SPECTAttenuationTransform(torch.tensor(mu_np, dtype=torch.float32),
+                                        assume_padded=False)]
+        if with_psf:
+            ts.append(SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)), assume_padded=False))
+        H = StarGuideSystemMatrix(om, pm, obj2obj_transforms=ts)
+        f = torch.tensor(f_true, dtype=torch.float32)
+        rec[f"{name}_fwd"] = H.forward(f).numpy()
+        rec[f"{name}_bwd"] = H.backward(proj).numpy()
+        H.set_n_subsets(2)
+        rec[f"{name}_subsets"] = np.concatenate([x.numpy() for x in H.subset_indices_array])
+        rec[f"{name}_fwd_s1"] = H.forward(f, 1).numpy()
+        rec[f"{name}_bwd_s1"] = H.backward(H.get_projection_subset(proj, 1), 1).numpy()
+        rec[f"{name}_norm_s0"] = H.compute_normalization_factor(0).numpy()
+    np.savez_compressed(os.path.join(out, "starguide.npz"), **rec)
+    print("wrote starguide", rec["att_psf_fwd"].shape, rec["att_subsets"])
+
+
 def theta_case(out):
     """Sampling matrices of the restated kornia rotation, for pinning the host tables."""
     rec = {}
@@ -442,6 +485,7 @@ def main():
     kem_filter_case(out)
     uncertainty_case(out)
     multibed_case(out)
+    starguide_case(out)
     print("pad sizes", {n: compute_pad_size(n) for n in (15, 16, 64, 96, 128)})
 
 

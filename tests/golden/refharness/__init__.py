@@ -86,7 +86,7 @@ class _PlaceholderFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
     def exec_module(self, module):
         if module.__name__ == "kornia.geometry.transform":
             module.rotate = kornia_rotate
-            module.Translate = _Anything
+            module.Translate = KorniaTranslate
 
 
 def kornia_rotate(tensor, angle, center=None, mode="bilinear", padding_mode="zeros",
@@ -101,6 +101,39 @@ def kornia_rotate(tensor, angle, center=None, mode="bilinear", padding_mode="zer
     grid = F.affine_grid(theta, [B, C, H, W], align_corners=align_corners)
     return F.grid_sample(tensor, grid, mode=mode, padding_mode=padding_mode,
                          align_corners=align_corners)
+
+
+class KorniaTranslate:
+    """Restatement of ``kornia.geometry.transform.Translate`` (used by
+    ``src/pytomography/projectors/SPECT/starguide_system_matrix.py:9,227``): the pixel
+    matrix ``[[1, 0, tx], [0, 1, ty]]`` per batch element, conjugated into normalised
+    coordinates like ``rotate`` and inverted, sampled with ``affine_grid`` /
+    ``grid_sample`` (bilinear, zero padding, ``align_corners=True``): the output at
+    column x is the input at column x - tx."""
+
+    def __init__(self, translation, mode="bilinear", padding_mode="zeros",
+                 align_corners=True):
+        self.translation = translation
+        self.mode, self.padding_mode, self.align_corners = mode, padding_mode, align_corners
+
+    def __call__(self, tensor):
+        B, C, H, W = tensor.shape
+        dt = tensor.dtype
+        t = torch.as_tensor(self.translation).to(dt).reshape(B, 2)
+        M = torch.eye(3, dtype=dt).repeat(B, 1, 1)
+        M[:, :2, 2] = t
+
+        def norm_pix(h, w):
+            tr = torch.tensor([[1.0, 0.0, -1.0], [0.0, 1.0, -1.0], [0.0, 0.0, 1.0]], dtype=dt)
+            tr[0, 0] = tr[0, 0] * 2.0 / (1e-14 if w == 1 else w - 1.0)
+            tr[1, 1] = tr[1, 1] * 2.0 / (1e-14 if h == 1 else h - 1.0)
+            return tr.unsqueeze(0)
+
+        n = norm_pix(H, W)
+        theta = torch.inverse(n @ M @ torch.inverse(n))[:, :2, :]
+        grid = F.affine_grid(theta, [B, C, H, W], align_corners=self.align_corners)
+        return F.grid_sample(tensor, grid, mode=self.mode, padding_mode=self.padding_mode,
+                             align_corners=self.align_corners)
 
 
 def kornia_sampling_matrix(angle: torch.Tensor, center: torch.Tensor, H: int, W: int):
