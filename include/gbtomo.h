@@ -100,7 +100,7 @@ int32_t gb_spect_subset_size(const gb_spect_plan *plan, int32_t subset);
  * fit shared memory; gb_spect_autotune times candidates on the device and keeps the
  * fastest.  No counterpart in the reference (which has no device code). */
 typedef struct gb_spect_tuning {
-    int32_t fwd_tpb;   /* threads per forward CTA: 512 (one CTA per SM) or 256 (two) */
+    int32_t fwd_tpb;   /* threads per forward CTA: 512 or 768 (one CTA per SM) */
     int32_t fwd_zt;    /* forward z-slab width; 0 = the widest that fits */
     int32_t fwd_items; /* forward work items per resident CTA slot and z slab: 1 or 2 */
     int32_t b1_zt;     /* back-projection (rotated frame) z-slab width; 0 = widest */

@@ -107,6 +107,61 @@ __device__ __forceinline__ void blur_second_acc(const float *__restrict__ Tt,
         for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
 }
 
+// Variants for CTAs whose register budget holds no tap registers (768-thread forward):
+// the taps are read from shared memory (a broadcast load) inside the tap loop.
+template <int K, int KK, int OB>
+__device__ __forceinline__ void blur_first_st(const float *__restrict__ S, float *__restrict__ Tt,
+                                              const float *__restrict__ tap, int SC, int TS,
+                                              int c_lo, int c_hi, int b_lo, int b_hi, int warp,
+                                              int lane, int nwarp) {
+    constexpr int OFF = (K - KK) / 2;
+    const int nb = b_hi - b_lo;
+    const int ncc = (c_hi - c_lo + 31) >> 5;
+    for (int p = warp; p < ncc * nb; p += nwarp) {
+        const int cc = p % ncc, yb = b_lo + p / ncc;
+        const int c = c_lo + (cc << 5) + lane;
+        if (c >= c_hi) continue;
+        const float *sp = S + (yb * OB + OFF) * SC + c;
+        float win[OB + KK - 1];
+#pragma unroll
+        for (int i = 0; i < OB + KK - 1; i++) win[i] = sp[i * SC];
+        float o[OB];
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = 0.f;
+#pragma unroll
+        for (int t = 0; t < KK; t++) {
+            const float wt = tap[OFF + t];
+#pragma unroll
+            for (int j = 0; j < OB; j++) o[j] = fmaf(wt, win[j + t], o[j]);
+        }
+        float *tq = Tt + c * TS + yb * OB;
+#pragma unroll
+        for (int j = 0; j < OB; j++) tq[j] = o[j];
+    }
+}
+
+// blur_second with shared-memory taps; ACC: o += blur instead of o = blur
+template <int K, int KK, int OB, bool ACC>
+__device__ __forceinline__ void blur_second_st(const float *__restrict__ Tt,
+                                               const float *__restrict__ wsm, int TS, int row0,
+                                               int col, float (&o)[OB]) {
+    constexpr int OFF = (K - KK) / 2;
+    const float *tq = Tt + (row0 + OFF) * TS + col;
+    float win[OB + KK - 1];
+#pragma unroll
+    for (int i = 0; i < OB + KK - 1; i++) win[i] = tq[i * TS];
+    if (!ACC) {
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = 0.f;
+    }
+#pragma unroll
+    for (int t = 0; t < KK; t++) {
+        const float wt = wsm[OFF + t];
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = fmaf(wt, win[j + t], o[j]);
+    }
+}
+
 template <int K, int KK>
 __device__ __forceinline__ void load_taps(const float *__restrict__ tap, float (&w)[KK]) {
     constexpr int OFF = (K - KK) / 2;

@@ -77,7 +77,8 @@ __global__ void k_reduce(const int *__restrict__ ioff, int NZ, const float *__re
 // ------------------------------------------------------------- launchers
 static bool fwd_fixed_host(int K, int N, int Zt, int tpb) {
     int OB = (K <= 31) ? 8 : 4;
-    return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= (tpb >= 512 ? 128 : 64);
+    (void)tpb;
+    return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= 128;
 }
 
 size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb) {
@@ -85,7 +86,7 @@ size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb) {
     int N8 = (N + OB - 1) / OB * OB;
     int Z8 = (Zt + OB - 1) / OB * OB;
     const bool fx = fwd_fixed_host(K, N, Zt, tpb);
-    const int ZW = tpb >= 512 ? 128 : 64;
+    const int ZW = 128;
     size_t SC = fx ? ZW + 2 * HP : Z8 + 2 * HP, TS = fx ? 129 : N8 + 1;
     return sizeof(float) * ((size_t)(N8 + 2 * H) * SC + (size_t)(Z8 + 2 * HP) * TS +
                             ((4 * K + 1) & ~1)) +

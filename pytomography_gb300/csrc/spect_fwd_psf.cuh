@@ -70,20 +70,23 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 //   taps [2][2][K]: double-buffered y / z taps of the current plane
 //   one mbarrier for the TMA copies
 // Per plane only the rows the rotated object square can reach are sampled / blurred.
-// FIXED: the tile fits 128 output rows and a z slab of at most ZW (128 for 512-thread
-// CTAs, 64 for 256-thread CTAs), so the shared-memory row strides are compile-time
-// constants (immediate-offset loads in the blur loops).
-// TPB: 512 threads and one CTA per SM, or 256 threads with a half-width z slab and two
-// CTAs per SM (one CTA's gathers overlap the other's blur arithmetic).
+// FIXED: the tile fits 128 output rows and a z slab of at most ZW = 128, so the
+// shared-memory row strides are compile-time constants (immediate-offset loads in the
+// blur loops).
+// TPB: 512 threads (16 warps), or 768 threads (24 warps: more rows of the gather in flight
+// per SM; the taps are read from shared memory to fit the smaller register budget).  One
+// CTA per SM either way.
 template <int K, bool VEC, bool FIXED, int TPB>
-__global__ void __launch_bounds__(TPB, 512 / TPB)
+__global__ void __launch_bounds__(TPB, 1)
     k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
               const int4 *__restrict__ items, int Zt, float *__restrict__ partials) {
     constexpr int H = K / 2;
-    constexpr int ZW = TPB >= 512 ? 128 : 64;
+    constexpr int ZW = 128;
+    constexpr bool TAPS_SMEM = TPB > 512;
     constexpr int HP = (H + 3) / 4 * 4;
     constexpr int OB = (K <= 31) ? 8 : 4;  // outputs per task
-    constexpr int NACC = 32 / OB;          // phase-3 tasks per thread
+    // phase-3 tasks per thread: 4 (OB = 8) or 8 with 512 threads; 3 or 6 with 768
+    constexpr int NACC = TPB > 512 ? (OB == 8 ? 3 : 6) : 32 / OB;
     const int4 item = items[blockIdx.x];  // (slot, first plane, end plane)
     const int slot = item.x;
     const int ga = alist[slot];
@@ -127,7 +130,20 @@ __global__ void __launch_bounds__(TPB, 512 / TPB)
     // each warp owns whole z blocks and, for them, every 32-row chunk: restricting a
     // plane's rows removes the same share of work from every warp
     // (falls back to a linear task order when the rows need more chunks than tasks)
-    {
+    if constexpr (TPB > 512) {
+        // linear warp-task order: task t = warp + nwarp k -> (32-row chunk t % n_yc, z block
+        // t / n_yc); the plan caps the slab so that every task has a thread
+        const int n_yc = (N8 + 31) >> 5, n_task = n_yc * (Z8 / OB);
+#pragma unroll
+        for (int k = 0; k < NACC; k++) {
+            const int t = warp + nwarp * k;
+            ty[k] = 32 * (t % n_yc) + lane;
+            tz[k] = t / n_yc;
+            if (t >= n_task || ty[k] >= N8) tz[k] = 1 << 20;  // no task
+#pragma unroll
+            for (int j = 0; j < OB; j++) acc[k][j] = 0.f;
+        }
+    } else {
         const int n_yc = (N8 + 31) >> 5;
         const bool balanced = n_yc <= NACC;
 #pragma unroll
@@ -213,14 +229,15 @@ __global__ void __launch_bounds__(TPB, 512 / TPB)
                 for (int q = lane; q < nq; q += 32)
                     *reinterpret_cast<float4 *>(Sr + 4 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            // four consecutive rows per warp and batch: neighbouring rows share about half
-            // of their bilinear taps, which then hit in L1
-            for (int y0 = ra + 4 * warp; y0 <= rb; y0 += 4 * nwarp) {
-                int ys[4];
-                bool okr[4];
-                Bilin b[4];
+            // RB consecutive rows per warp and batch (4 with 512 threads, 2 with 768):
+            // neighbouring rows share about half of their bilinear taps, which then hit in L1
+            constexpr int RB = TAPS_SMEM ? 2 : 4;
+            for (int y0 = ra + RB * warp; y0 <= rb; y0 += RB * nwarp) {
+                int ys[RB];
+                bool okr[RB];
+                Bilin b[RB];
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
+                for (int u = 0; u < RB; u++) {
                     ys[u] = y0 + u;
                     okr[u] = ys[u] <= rb;
                     float ix, iy;
@@ -229,13 +246,13 @@ __global__ void __launch_bounds__(TPB, 512 / TPB)
                 }
                 for (int q = lane; q < nq; q += 32) {
                     const int z = zq_lo + 4 * q;
-                    float4 v[4];
-                    bool h[4];
+                    float4 v[RB];
+                    bool h[RB];
 #pragma unroll
-                    for (int u = 0; u < 4; u++)
+                    for (int u = 0; u < RB; u++)
                         h[u] = okr[u] && sample4(f, N, N, nz, g.pad, g.pad, b[u], z, v[u]);
 #pragma unroll
-                    for (int u = 0; u < 4; u++) {
+                    for (int u = 0; u < RB; u++) {
                         if (!okr[u]) continue;
                         float4 *dst = reinterpret_cast<float4 *>(
                             S + (ys[u] - (g.pad - H)) * SC + qcol0 + 4 * q);
@@ -280,7 +297,12 @@ __global__ void __launch_bounds__(TPB, 512 / TPB)
         if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : kTiers - 1;
         tier_dispatch<K>(tier, [&](auto kk) {
             constexpr int KK = decltype(kk)::value;
-            blur_first<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
+            if constexpr (TAPS_SMEM)
+                blur_first_st<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
+                                         nwarp);
+            else
+                blur_first<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
+                                      nwarp);
         });
         GB_T(6, rb - ra + 1);
         GB_T(7, (b_hi - b_lo) * OB * tier_taps(K, tier));
@@ -304,19 +326,27 @@ __global__ void __launch_bounds__(TPB, 512 / TPB)
             const bool post_att = Ap && !g.att_first;
             tier_dispatch<K>(tier, [&](auto kk) {
                 constexpr int KK = decltype(kk)::value;
-                float w[KK];
-                load_taps<K, KK>(tap + K, w);
+                float w[TAPS_SMEM ? 1 : KK];
+                if constexpr (!TAPS_SMEM) load_taps<K, KK>(tap + K, w);
 #pragma unroll
                 for (int k = 0; k < NACC; k++) {
                     const int y = ty[k], zb = tz[k];
                     if (zb * OB < Z8 && y >= y_lo && y < y_hi) {
                         if (g.psf2d && !post_att) {
-                            blur_second_acc<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, acc[k]);
+                            if constexpr (TAPS_SMEM)
+                                blur_second_st<K, KK, OB, true>(Tt, tap + K, TS, zb * OB + HP - H,
+                                                                y, acc[k]);
+                            else
+                                blur_second_acc<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, acc[k]);
                             continue;
                         }
                         float o[OB];
                         if (g.psf2d) {
-                            blur_second<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, o);
+                            if constexpr (TAPS_SMEM)
+                                blur_second_st<K, KK, OB, false>(Tt, tap + K, TS,
+                                                                 zb * OB + HP - H, y, o);
+                            else
+                                blur_second<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, o);
                         } else {
 #pragma unroll
                             for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + HP) * TS + y];
@@ -372,7 +402,8 @@ __global__ void __launch_bounds__(TPB, 512 / TPB)
 // ------------------------------------------------------------- launchers
 inline bool fwd_fixed(int K, int N, int Zt, int tpb) {
     int OB = (K <= 31) ? 8 : 4;
-    return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= (tpb >= 512 ? 128 : 64);
+    (void)tpb;
+    return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= 128;
 }
 
 template <int K, int TPB>
@@ -417,12 +448,12 @@ inline cudaError_t setup_fwd_t(size_t smem) {
     cudaError_t launch_fwd_psf_##KK(const SpectDev &g, const float *f, const int *alist,     \
                                     const int4 *items, int n_items, int Zt, int tpb,         \
                                     float *partials, cudaStream_t st) {                     \
-        return tpb >= 512                                                                    \
+        return tpb <= 512                                                                    \
                    ? launch_fwd_psf_t<KK, 512>(g, f, alist, items, n_items, Zt, partials, st) \
-                   : launch_fwd_psf_t<KK, 256>(g, f, alist, items, n_items, Zt, partials, st); \
+                   : launch_fwd_psf_t<KK, 768>(g, f, alist, items, n_items, Zt, partials, st); \
     }                                                                                        \
     cudaError_t setup_fwd_##KK(size_t smem, int tpb) {                                       \
-        return tpb >= 512 ? setup_fwd_t<KK, 512>(smem) : setup_fwd_t<KK, 256>(smem);         \
+        return tpb <= 512 ? setup_fwd_t<KK, 512>(smem) : setup_fwd_t<KK, 768>(smem);         \
     }
 
 }  // namespace gb

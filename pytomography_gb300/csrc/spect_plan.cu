@@ -38,17 +38,6 @@ static size_t max_smem_optin() {
     return v > 0 ? (size_t)v : 227 * 1024;
 }
 
-// Shared memory one CTA may use when `per_sm` CTAs share an SM.
-static size_t smem_cap(int per_sm) {
-    if (per_sm <= 1) return max_smem_optin();
-    int dev = 0, sm = 0, res = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    cudaDeviceGetAttribute(&res, cudaDevAttrReservedSharedMemoryPerBlock, dev);
-    if (sm <= 0) sm = 228 * 1024;
-    return std::min(max_smem_optin(), (size_t)(sm / per_sm - res));
-}
-
 }  // namespace gb
 
 using namespace gb;
@@ -89,7 +78,7 @@ struct gb_spect_plan {
     int2 *d_wrange = nullptr;
     int *d_err = nullptr;
     int Zt_fwd = 0, Zt_b1 = 0;
-    int fwd_tpb = 512;  // forward CTA size: 512 (one CTA per SM) or 256 (two per SM)
+    int fwd_tpb = 512;  // forward CTA size: 512 or 768 threads (one CTA per SM)
     int fwd_items = 1, b1_items = 1;  // work items per resident CTA slot and z slab
 };
 
@@ -276,7 +265,7 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
         if (psf) {
             std::vector<double> wa(L.n);
             for (int i = 0; i < L.n; i++) wa[i] = sum_of(wf[l[i]]);
-            std::vector<int> cnt = chunk_counts(p, wa, zs_f, (512 / p->fwd_tpb) * p->fwd_items);
+            std::vector<int> cnt = chunk_counts(p, wa, zs_f, p->fwd_items);
             for (int i = 0; i < L.n; i++) {
                 ioff.push_back((int)items.size() - L.fitem_off);
                 split_planes(wf[l[i]], cnt[i], i, items);
@@ -348,16 +337,19 @@ static bool select_list(const gb_spect_plan *p, int subset, const int **alist, i
 
 // z-slab width for the PSF kernels: the largest multiple of the output block that fits
 // shared memory (and, for the forward, the 32 accumulator registers per thread of a
-// `tpb`-thread CTA; with 256 threads two CTAs share an SM).
+// `tpb`-thread CTA: 512 or 768 threads, one CTA per SM).
 static int choose_zt(int K, int N, int nz, bool fwd, int tpb = 512) {
     int OB = (K <= 31) ? 8 : 4;
-    size_t cap = fwd ? smem_cap(512 / tpb) : max_smem_optin();
+    size_t cap = max_smem_optin();
     int best = 0;
     for (int zt = OB; zt < nz + OB; zt += OB) {
         int z = std::min(zt, (nz + OB - 1) / OB * OB);
         size_t sm = fwd ? fwd_psf_smem_bytes(K, N, z, tpb) : b1_psf_smem_bytes(K, N, z);
         if (sm > cap) break;
-        if (fwd) {  // phase-3 tasks of k_fwd_psf: tpb / 32 warps x (32 / OB) tasks per thread
+        if (fwd && tpb > 512) {  // 768 threads: 24 warps x (3 or 6) linear warp-tasks
+            const int N8 = (N + OB - 1) / OB * OB, n_yc = (N8 + 31) / 32;
+            if ((long)n_yc * (z / OB) > 24L * (OB == 8 ? 3 : 6)) break;
+        } else if (fwd) {  // phase-3 tasks of k_fwd_psf: 16 warps x (32 / OB) tasks per thread
             const int N8 = (N + OB - 1) / OB * OB, NACC = 32 / OB, n_yc = (N8 + 31) / 32;
             if (n_yc <= NACC) {
                 if (z / OB > (tpb / 32) * (NACC / n_yc)) break;
@@ -623,7 +615,7 @@ gb_status gb_spect_get_tuning(const gb_spect_plan *p, gb_spect_tuning *out) {
 // Check a tuning against the plan's limits and fill in the z slabs left at 0.
 static gb_status resolve_tuning(const gb_spect_plan *p, gb_spect_tuning &t) {
     const int K = p->dev.K, OB = (K <= 31) ? 8 : 4;
-    GB_CHECK_ARG(t.fwd_tpb == 512 || t.fwd_tpb == 256, "fwd_tpb must be 512 or 256");
+    GB_CHECK_ARG(t.fwd_tpb == 512 || t.fwd_tpb == 768, "fwd_tpb must be 512 or 768");
     GB_CHECK_ARG(t.fwd_items >= 1 && t.fwd_items <= 2 && t.b1_items >= 1 && t.b1_items <= 2,
                  "items per SM must be 1 or 2");
     const int zf = choose_zt(K, p->N, p->nz, true, t.fwd_tpb);
@@ -730,8 +722,8 @@ gb_status gb_spect_backward(gb_spect_plan *p, const float *proj, float *obj, int
 
 // Autotuner: time each candidate tile configuration of the forward kernel, then of the
 // back-projection kernel, on a temporary object of ones and keep the fastest.  The
-// candidates are the CTA size (512 threads, or 256 threads with two CTAs per SM when its
-// tile fits), the widest z slab and half of it, and one or two work items per CTA slot.
+// candidates are the CTA size (512 threads, or 768 threads with the taps in shared memory),
+// the widest z slab and half of it, and one or two work items per CTA slot.
 gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
                             gb_spect_tuning *out, gb_stream_t stream) {
     clear_error();
@@ -796,7 +788,7 @@ gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
     // forward candidates
     float best_ms = 1e30f;
     gb_spect_tuning fbest = best;
-    for (int tpb : {512, 256}) {
+    for (int tpb : {512, 768}) {
         const int zmax = choose_zt(K, p->N, p->nz, true, tpb);
         if (!zmax) continue;
         for (int zt : {zmax, (zmax / 2) / OB * OB}) {

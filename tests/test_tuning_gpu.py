@@ -43,7 +43,7 @@ def test_every_tuning_matches_oracle(cuda):
     gt = torch.tensor(g, dtype=torch.float32, device=cuda)
     default = H.get_tuning()
     seen = 0
-    for tpb in (512, 256):
+    for tpb in (512, 768):
         for zt in (0, 48):
             for items in (1, 2):
                 try:
@@ -69,7 +69,7 @@ def test_autotune_picks_a_valid_tuning_and_caches(cuda):
     ft = torch.tensor(f, dtype=torch.float32, device=cuda)
     before = H.forward(ft, 2)
     t = H.autotune(0)
-    assert t["fwd_tpb"] in (256, 512) and t["fwd_items"] in (1, 2)
+    assert t["fwd_tpb"] in (512, 768) and t["fwd_items"] in (1, 2)
     assert H.get_tuning() == t
     after = H.forward(ft, 2)
     assert float((after - before).norm() / before.norm()) < 1e-6
