@@ -162,6 +162,77 @@ __device__ __forceinline__ void blur_second_st(const float *__restrict__ Tt,
     }
 }
 
+// Column-pair variants (fma.rn.f32x2): a thread owns two neighbouring columns and every
+// tap is one packed FMA over both.  Each component is the same fmaf chain, in the same tap
+// order, as the scalar passes above (identical results) with half the FMA and shared-load
+// instructions.  Row strides and the first column must be even (8-byte float2 access).
+
+// First pass over column pairs [c_lo & ~1, (c_hi + 1) & ~1): the extra edge column reads
+// S zeros or samples outside the z range the second pass uses.  Warp-tasks are (64-column
+// chunk, row block); the transposed output of the two columns goes out as float2 pairs.
+template <int K, int KK, int OB>
+__device__ __forceinline__ void blur_first2(const float *__restrict__ S, float *__restrict__ Tt,
+                                            const float *__restrict__ tap, int SC, int TS,
+                                            int c_lo, int c_hi, int b_lo, int b_hi, int warp,
+                                            int lane, int nwarp) {
+    static_assert(OB % 2 == 0, "pair stores need an even row block");
+    constexpr int OFF = (K - KK) / 2;
+    float w[KK];
+#pragma unroll
+    for (int t = 0; t < KK; t++) w[t] = tap[OFF + t];
+    const int c0 = c_lo & ~1, c1 = (c_hi + 1) & ~1;
+    const int nb = b_hi - b_lo;
+    const int ncc = (c1 - c0 + 63) >> 6;
+    const int SC2 = SC >> 1;
+    for (int p = warp; p < ncc * nb; p += nwarp) {
+        const int cc = p % ncc, yb = b_lo + p / ncc;
+        const int c = c0 + (cc << 6) + 2 * lane;
+        if (c >= c1) continue;
+        const float2 *sp = reinterpret_cast<const float2 *>(S + (yb * OB + OFF) * SC + c);
+        float2 win[OB + KK - 1];
+#pragma unroll
+        for (int i = 0; i < OB + KK - 1; i++) win[i] = sp[i * SC2];
+        float2 o[OB];
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < KK; t++) {
+            const float2 wt = make_float2(w[t], w[t]);
+#pragma unroll
+            for (int j = 0; j < OB; j++) o[j] = __ffma2_rn(wt, win[j + t], o[j]);
+        }
+        float *tq = Tt + c * TS + yb * OB;
+#pragma unroll
+        for (int j = 0; j < OB; j += 2) {
+            *reinterpret_cast<float2 *>(tq + j) = make_float2(o[j].x, o[j + 1].x);
+            *reinterpret_cast<float2 *>(tq + TS + j) = make_float2(o[j].y, o[j + 1].y);
+        }
+    }
+}
+
+// Second pass of one task over the column pair (col, col + 1), col even; ACC: o += blur.
+template <int K, int KK, int OB, bool ACC>
+__device__ __forceinline__ void blur_second2(const float *__restrict__ Tt,
+                                             const float (&w)[KK], int TS, int row0, int col,
+                                             float2 (&o)[OB]) {
+    constexpr int OFF = (K - KK) / 2;
+    const float2 *tq = reinterpret_cast<const float2 *>(Tt + (row0 + OFF) * TS + col);
+    const int TS2 = TS >> 1;
+    float2 win[OB + KK - 1];
+#pragma unroll
+    for (int i = 0; i < OB + KK - 1; i++) win[i] = tq[i * TS2];
+    if (!ACC) {
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int t = 0; t < KK; t++) {
+        const float2 wt = make_float2(w[t], w[t]);
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = __ffma2_rn(wt, win[j + t], o[j]);
+    }
+}
+
 template <int K, int KK>
 __device__ __forceinline__ void load_taps(const float *__restrict__ tap, float (&w)[KK]) {
     constexpr int OFF = (K - KK) / 2;

@@ -87,7 +87,9 @@ size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb) {
     int Z8 = (Zt + OB - 1) / OB * OB;
     const bool fx = fwd_fixed_host(K, N, Zt, tpb);
     const int ZW = 128;
-    size_t SC = fx ? ZW + 2 * HP : Z8 + 2 * HP, TS = fx ? 129 : N8 + 1;
+    // Tt row stride: even (float2 row pairs) with 512 threads, odd with 768
+    const int ts_pad = tpb <= 512 ? 2 : 1;
+    size_t SC = fx ? ZW + 2 * HP : Z8 + 2 * HP, TS = fx ? 128 + ts_pad : N8 + ts_pad;
     return sizeof(float) * ((size_t)(N8 + 2 * H) * SC + (size_t)(Z8 + 2 * HP) * TS +
                             ((4 * K + 1) & ~1)) +
            sizeof(unsigned long long);

@@ -85,8 +85,12 @@ __global__ void __launch_bounds__(TPB, 1)
     constexpr bool TAPS_SMEM = TPB > 512;
     constexpr int HP = (H + 3) / 4 * 4;
     constexpr int OB = (K <= 31) ? 8 : 4;  // outputs per task
-    // phase-3 tasks per thread: 4 (OB = 8) or 8 with 512 threads; 3 or 6 with 768
-    constexpr int NACC = TPB > 512 ? (OB == 8 ? 3 : 6) : 32 / OB;
+    // phase-3 tasks per thread.  512 threads: a task owns a pair of output rows (y, y + 1)
+    // and blurs both with packed f32x2 FMAs, 2 (OB = 8) or 4 tasks; 768 threads: one row
+    // per task, 3 or 6 tasks
+    constexpr bool PAIR = !TAPS_SMEM;
+    constexpr int NT = PAIR ? 16 / OB : (OB == 8 ? 3 : 6);
+    using Acc = std::conditional_t<PAIR, float2, float>;
     const int4 item = items[blockIdx.x];  // (slot, first plane, end plane)
     const int slot = item.x;
     const int ga = alist[slot];
@@ -95,9 +99,10 @@ __global__ void __launch_bounds__(TPB, 1)
     const int Zc = min(Zt, nz - z0);
     const int N8 = (N + OB - 1) / OB * OB;
     const int Z8 = (Zc + OB - 1) / OB * OB;
-    constexpr int SC_FIX = ZW + 2 * HP, TS_FIX = 129;
+    // Tt row stride: odd for scalar access (conflict-free columns), even for float2 pairs
+    constexpr int SC_FIX = ZW + 2 * HP, TS_FIX = PAIR ? 130 : 129;
     const int SC = FIXED ? SC_FIX : Z8 + 2 * HP, SR = N8 + 2 * H;
-    const int TS = FIXED ? TS_FIX : N8 + 1, TR = Z8 + 2 * HP;
+    const int TS = FIXED ? TS_FIX : N8 + (PAIR ? 2 : 1), TR = Z8 + 2 * HP;
     extern __shared__ __align__(128) float sm[];
     float *S = sm;
     float *Tt = S + SR * SC;
@@ -125,8 +130,8 @@ __global__ void __launch_bounds__(TPB, 1)
     const unsigned row_bytes = (unsigned)(zq_hi - zq_lo) * 4u;
     const int qcol0 = zq_lo - z0 + HP;  // S column of the first quad
     if (threadIdx.x == 0 && use_tma) mbar_init(bar, 1);
-    float acc[NACC][OB];
-    int ty[NACC], tz[NACC];  // phase-3 task (output row, z block) of this thread
+    Acc acc[NT][OB];
+    int ty[NT], tz[NT];  // phase-3 task (output row or first row of a pair, z block)
     // each warp owns whole z blocks and, for them, every 32-row chunk: restricting a
     // plane's rows removes the same share of work from every warp
     // (falls back to a linear task order when the rows need more chunks than tasks)
@@ -135,30 +140,32 @@ __global__ void __launch_bounds__(TPB, 1)
         // t / n_yc); the plan caps the slab so that every task has a thread
         const int n_yc = (N8 + 31) >> 5, n_task = n_yc * (Z8 / OB);
 #pragma unroll
-        for (int k = 0; k < NACC; k++) {
+        for (int k = 0; k < NT; k++) {
             const int t = warp + nwarp * k;
             ty[k] = 32 * (t % n_yc) + lane;
             tz[k] = t / n_yc;
             if (t >= n_task || ty[k] >= N8) tz[k] = 1 << 20;  // no task
 #pragma unroll
-            for (int j = 0; j < OB; j++) acc[k][j] = 0.f;
+            for (int j = 0; j < OB; j++) acc[k][j] = Acc{};
         }
     } else {
-        const int n_yc = (N8 + 31) >> 5;
-        const bool balanced = n_yc <= NACC;
+        // row pairs: lanes take consecutive pairs of a 64-row chunk
+        const int n_yc = (N8 + 63) >> 6;
+        const bool balanced = n_yc <= NT;
 #pragma unroll
-        for (int k = 0; k < NACC; k++) {
+        for (int k = 0; k < NT; k++) {
             if (balanced) {
-                ty[k] = 32 * (k % n_yc) + lane;
+                ty[k] = 64 * (k % n_yc) + 2 * lane;
                 tz[k] = warp + nwarp * (k / n_yc);
-                if (ty[k] >= N8 || k / n_yc >= NACC / n_yc) tz[k] = 1 << 20;  // no task
+                if (ty[k] >= N8 || k / n_yc >= NT / n_yc) tz[k] = 1 << 20;  // no task
             } else {
+                const int np = N8 >> 1;  // row pairs per z block
                 const int task = threadIdx.x + k * TPB;
-                ty[k] = task % N8;
-                tz[k] = task / N8;
+                ty[k] = 2 * (task % np);
+                tz[k] = task / np;
             }
 #pragma unroll
-            for (int j = 0; j < OB; j++) acc[k][j] = 0.f;
+            for (int j = 0; j < OB; j++) acc[k][j] = Acc{};
         }
     }
     __syncthreads();
@@ -301,8 +308,8 @@ __global__ void __launch_bounds__(TPB, 1)
                 blur_first_st<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
                                          nwarp);
             else
-                blur_first<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
-                                      nwarp);
+                blur_first2<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
+                                       nwarp);
         });
         GB_T(6, rb - ra + 1);
         GB_T(7, (b_hi - b_lo) * OB * tier_taps(K, tier));
@@ -326,42 +333,74 @@ __global__ void __launch_bounds__(TPB, 1)
             const bool post_att = Ap && !g.att_first;
             tier_dispatch<K>(tier, [&](auto kk) {
                 constexpr int KK = decltype(kk)::value;
-                float w[TAPS_SMEM ? 1 : KK];
-                if constexpr (!TAPS_SMEM) load_taps<K, KK>(tap + K, w);
+                if constexpr (PAIR) {
+                    float w[KK];
+                    load_taps<K, KK>(tap + K, w);
 #pragma unroll
-                for (int k = 0; k < NACC; k++) {
-                    const int y = ty[k], zb = tz[k];
-                    if (zb * OB < Z8 && y >= y_lo && y < y_hi) {
-                        if (g.psf2d && !post_att) {
-                            if constexpr (TAPS_SMEM)
-                                blur_second_st<K, KK, OB, true>(Tt, tap + K, TS, zb * OB + HP - H,
-                                                                y, acc[k]);
-                            else
-                                blur_second_acc<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, acc[k]);
-                            continue;
-                        }
-                        float o[OB];
-                        if (g.psf2d) {
-                            if constexpr (TAPS_SMEM)
-                                blur_second_st<K, KK, OB, false>(Tt, tap + K, TS,
-                                                                 zb * OB + HP - H, y, o);
-                            else
-                                blur_second<K, KK, OB>(Tt, w, TS, zb * OB + HP - H, y, o);
-                        } else {
+                    for (int k = 0; k < NT; k++) {
+                        const int y = ty[k], zb = tz[k];  // rows y, y + 1 (y_lo, y_hi even)
+                        if (zb * OB < Z8 && y >= y_lo && y < y_hi) {
+                            if (g.psf2d && !post_att) {
+                                blur_second2<K, KK, OB, true>(Tt, w, TS, zb * OB + HP - H, y,
+                                                              acc[k]);
+                                continue;
+                            }
+                            float2 o[OB];
+                            if (g.psf2d) {
+                                blur_second2<K, KK, OB, false>(Tt, w, TS, zb * OB + HP - H, y, o);
+                            } else {
 #pragma unroll
-                            for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + HP) * TS + y];
-                        }
-                        if (post_att && y < N) {
+                                for (int j = 0; j < OB; j++)
+                                    o[j] = *reinterpret_cast<const float2 *>(
+                                        Tt + (zb * OB + j + HP) * TS + y);
+                            }
+                            if (post_att) {
+#pragma unroll
+                                for (int j = 0; j < OB; j++) {
+                                    const int z = z0 + zb * OB + j;
+                                    if (z >= nz) continue;
+                                    const float *Az = Ap + (size_t)(g.pad + y - g.ya_lo) * nz + z;
+                                    if (y < N) o[j].x = __fmul_rn(o[j].x, Az[0]);
+                                    if (y + 1 < N) o[j].y = __fmul_rn(o[j].y, Az[nz]);
+                                }
+                            }
 #pragma unroll
                             for (int j = 0; j < OB; j++) {
-                                const int z = z0 + zb * OB + j;
-                                if (z < nz)
-                                    o[j] = __fmul_rn(o[j],
-                                                     Ap[(size_t)(g.pad + y - g.ya_lo) * nz + z]);
+                                acc[k][j].x += o[j].x;
+                                acc[k][j].y += o[j].y;
                             }
                         }
+                    }
+                } else {  // 768 threads: one output row per task, taps from shared memory
 #pragma unroll
-                        for (int j = 0; j < OB; j++) acc[k][j] += o[j];
+                    for (int k = 0; k < NT; k++) {
+                        const int y = ty[k], zb = tz[k];
+                        if (zb * OB < Z8 && y >= y_lo && y < y_hi) {
+                            if (g.psf2d && !post_att) {
+                                blur_second_st<K, KK, OB, true>(Tt, tap + K, TS, zb * OB + HP - H,
+                                                                y, acc[k]);
+                                continue;
+                            }
+                            float o[OB];
+                            if (g.psf2d) {
+                                blur_second_st<K, KK, OB, false>(Tt, tap + K, TS, zb * OB + HP - H,
+                                                                 y, o);
+                            } else {
+#pragma unroll
+                                for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + HP) * TS + y];
+                            }
+                            if (post_att && y < N) {
+#pragma unroll
+                                for (int j = 0; j < OB; j++) {
+                                    const int z = z0 + zb * OB + j;
+                                    if (z < nz)
+                                        o[j] = __fmul_rn(o[j],
+                                                         Ap[(size_t)(g.pad + y - g.ya_lo) * nz + z]);
+                                }
+                            }
+#pragma unroll
+                            for (int j = 0; j < OB; j++) acc[k][j] += o[j];
+                        }
                     }
                 }
             });
@@ -387,13 +426,19 @@ __global__ void __launch_bounds__(TPB, 1)
     // partial ray sums of this item
     float *out = partials + (size_t)blockIdx.x * N * nz;
 #pragma unroll
-    for (int k = 0; k < NACC; k++) {
+    for (int k = 0; k < NT; k++) {
         const int y = ty[k], zb = tz[k];
         if (zb * OB < Z8 && y < N) {
 #pragma unroll
             for (int j = 0; j < OB; j++) {
                 int z = z0 + zb * OB + j;
-                if (z - z0 < Zc) out[(size_t)y * nz + z] = acc[k][j];
+                if (z - z0 >= Zc) continue;
+                if constexpr (PAIR) {
+                    out[(size_t)y * nz + z] = acc[k][j].x;
+                    if (y + 1 < N) out[(size_t)(y + 1) * nz + z] = acc[k][j].y;
+                } else {
+                    out[(size_t)y * nz + z] = acc[k][j];
+                }
             }
         }
     }

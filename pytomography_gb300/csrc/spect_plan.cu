@@ -349,11 +349,11 @@ static int choose_zt(int K, int N, int nz, bool fwd, int tpb = 512) {
         if (fwd && tpb > 512) {  // 768 threads: 24 warps x (3 or 6) linear warp-tasks
             const int N8 = (N + OB - 1) / OB * OB, n_yc = (N8 + 31) / 32;
             if ((long)n_yc * (z / OB) > 24L * (OB == 8 ? 3 : 6)) break;
-        } else if (fwd) {  // phase-3 tasks of k_fwd_psf: 16 warps x (32 / OB) tasks per thread
-            const int N8 = (N + OB - 1) / OB * OB, NACC = 32 / OB, n_yc = (N8 + 31) / 32;
-            if (n_yc <= NACC) {
-                if (z / OB > (tpb / 32) * (NACC / n_yc)) break;
-            } else if ((long)N8 * (z / OB) > (long)tpb * NACC) {
+        } else if (fwd) {  // phase-3 tasks of k_fwd_psf: 16 warps x (16 / OB) row-pair tasks
+            const int N8 = (N + OB - 1) / OB * OB, NT = 16 / OB, n_yc = (N8 + 63) / 64;
+            if (n_yc <= NT) {
+                if (z / OB > (tpb / 32) * (NT / n_yc)) break;
+            } else if ((long)(N8 / 2) * (z / OB) > (long)tpb * NT) {
                 break;
             }
         }
