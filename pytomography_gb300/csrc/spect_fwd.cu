@@ -6,6 +6,10 @@
 // with SPECTAttenuationTransform.forward (transforms/SPECT/attenuation.py:72-92); the
 // ratio epilogue is PoissonLogLikelihood.compute_gradient's g / (H f + s + delta)
 // (likelihoods/poisson_log_likelihood.py:33-36).
+#include <cudaTypedefs.h>
+
+#include <cstring>
+
 #include "spect_kernels.cuh"
 #include "spect_launch.h"
 
@@ -89,13 +93,44 @@ size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb) {
     const int ZW = 128;
     // Tt row stride: even (float2 row pairs) with 512 threads, odd with 768
     const int ts_pad = tpb <= 512 ? 2 : 1;
-    size_t SC = fx ? ZW + 2 * HP : Z8 + 2 * HP, TS = fx ? 128 + ts_pad : N8 + ts_pad;
+    size_t SC = fwd_s_cols(fx ? ZW : Z8, HP), TS = fx ? 128 + ts_pad : N8 + ts_pad;
     return sizeof(float) * ((size_t)(N8 + 2 * H) * SC + (size_t)(Z8 + 2 * HP) * TS +
                             ((4 * K + 1) & ~1)) +
            sizeof(unsigned long long);
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+cudaError_t make_att_tmap(const SpectDev &g, int s_cols, CUtensorMap *out) {
+    std::memset(out, 0, sizeof(*out));
+    // the kernel copies boxes only for an attenuation-first table with z quads
+    if (!g.att || !g.att_first || !g.A || g.nz % 4 != 0 || s_cols > 256) return cudaSuccess;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    const cuuint64_t dims[2] = {(cuuint64_t)g.nz, (cuuint64_t)g.n_angles * g.Lp * g.nya};
+    const cuuint64_t strides[1] = {(cuuint64_t)g.nz * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)s_cols, (cuuint32_t)kBoxRows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(g.A), dims,
+                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t setup_fwd(int K, size_t smem, int tpb) {
+    (void)tensor_map_encoder();  // driver lookup outside any stream capture
     switch (K) {
 #define GB_SETUP_CASE(KK) \
     case KK:              \

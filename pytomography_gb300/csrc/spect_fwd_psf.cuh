@@ -20,12 +20,14 @@
 namespace gb {
 
 #ifdef GB_PHASE_TIMING
-// Per-CTA cycle counts of the forward kernel's phases (diagnostic builds only, written to
-// g.phase when set): [0] waits for the attenuation copy, [1] phase 1, [2] phase 2,
-// [3] phase 3, [4] planes processed, [5] total, [6] rows sampled, [7] output rows x taps.
+// Per-warp cycle counts of the forward kernel's phases (diagnostic builds only, written to
+// g.phase[(CTA * warps + warp) * 8 + k] when set): [0] waits for the attenuation copy,
+// [1] phase 1 work, [2] wait at the barrier after phase 1, [3] phase 2 work, [4] wait at
+// the barrier after phase 2, [5] phase 3 work (with the next plane's copy issue),
+// [6] planes processed, [7] total.
 #define GB_T(k, v)                                              \
     do {                                                        \
-        if (threadIdx.x == 0) tacc[k] += (v);                   \
+        if ((threadIdx.x & 31) == 0) tacc[k] += (v);            \
     } while (0)
 #define GB_NOW() clock64()
 #else
@@ -64,8 +66,10 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 // Shared-memory layout (per CTA):
 //   S  [SR][SC]: rotated, attenuated samples; row r <-> padded y = pad - H + r,
 //                column c <-> z = z0 - HP + c  (HP = H rounded up to 4: 16-byte aligned
-//                z quads).  Before phase 1 of a plane, the attenuation rows of that
-//                plane are bulk-copied (TMA) into S and multiplied in place.
+//                z quads; SC a multiple of 32: 128-byte aligned rows).  Before phase 1 of
+//                a plane, the attenuation rows of that plane are copied into S by 2-D TMA
+//                boxes of kBoxRows full S rows (`tmA`: A viewed as [n_angles*Lp*nya][nz],
+//                z outside [0, nz) reads as zero) and multiplied in place.
 //   Tt [TR][TS]: y-blurred plane, transposed; row c <-> z = z0 - HP + c, column = output y
 //   taps [2][2][K]: double-buffered y / z taps of the current plane
 //   one mbarrier for the TMA copies
@@ -79,7 +83,8 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 template <int K, bool VEC, bool FIXED, int TPB>
 __global__ void __launch_bounds__(TPB, 1)
     k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
-              const int4 *__restrict__ items, int Zt, float *__restrict__ partials) {
+              const int4 *__restrict__ items, int Zt, float *__restrict__ partials,
+              const __grid_constant__ CUtensorMap tmA) {
     constexpr int H = K / 2;
     constexpr int ZW = 128;
     constexpr bool TAPS_SMEM = TPB > 512;
@@ -100,8 +105,8 @@ __global__ void __launch_bounds__(TPB, 1)
     const int N8 = (N + OB - 1) / OB * OB;
     const int Z8 = (Zc + OB - 1) / OB * OB;
     // Tt row stride: odd for scalar access (conflict-free columns), even for float2 pairs
-    constexpr int SC_FIX = ZW + 2 * HP, TS_FIX = PAIR ? 130 : 129;
-    const int SC = FIXED ? SC_FIX : Z8 + 2 * HP, SR = N8 + 2 * H;
+    constexpr int SC_FIX = fwd_s_cols(ZW, HP), TS_FIX = PAIR ? 130 : 129;
+    const int SC = FIXED ? SC_FIX : fwd_s_cols((Zt + OB - 1) / OB * OB, HP), SR = N8 + 2 * H;
     const int TS = FIXED ? TS_FIX : N8 + (PAIR ? 2 : 1), TR = Z8 + 2 * HP;
     extern __shared__ __align__(128) float sm[];
     float *S = sm;
@@ -118,6 +123,7 @@ __global__ void __launch_bounds__(TPB, 1)
     const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
     const bool amul = A && g.att_first;
     const bool use_tma = VEC && amul;
+    const bool tma_box = SC <= 256;  // 2-D boxes (else one 1-D copy per row)
     const int x0 = item.y, x1 = item.z;
     const int zv_lo = max(0, z0 - H), zv_hi = min(nz, z0 + Zc + H);  // z needed by the blur
     const int cz_lo = zv_lo - z0 + HP, cz_hi = zv_hi - z0 + HP;
@@ -178,23 +184,44 @@ __global__ void __launch_bounds__(TPB, 1)
             if (plane_rows(g, th, xp, ylo, yhi, 0.5f, ra, rb)) return xp;
         return x1;
     };
-    // bulk-copy the attenuation rows [ra, rb] of plane xp into S (warp 0)
-    auto issue_tma = [&](int xp, int ra, int rb) {
+    // copy the attenuation rows [ra, rb] of plane xp into S (warp 0).  Boxes start at ra,
+    // ra + kBoxRows, ...; the last one ends at rb, or starts at ylo when the range is
+    // shorter than a box, so the rows written are [fa, fb] (rows outside [ra, rb] are
+    // cleared in phase 1).
+    auto issue_tma = [&](int xp, int ra, int rb, int &fa, int &fb) {
+        const int nbox = (rb - ra + kBoxRows) / kBoxRows;
+        const int last = max(ylo, rb - (kBoxRows - 1));
+        fa = ra;
+        fb = rb;
+        if (tma_box) {
+            fa = min(ra, last);
+            fb = max(rb, last + kBoxRows - 1);
+        }
         if (warp != 0 || __any_sync(0xffffffffu, failed)) return;
         if (lane == 0) {
             fence_proxy_async_smem();
-            mbar_arrive_expect_tx(bar, row_bytes * (unsigned)(rb - ra + 1));
+            mbar_arrive_expect_tx(bar, tma_box ? (unsigned)(nbox * kBoxRows * SC) * 4u
+                                               : row_bytes * (unsigned)(rb - ra + 1));
         }
         __syncwarp();
-        const float *src = A + ((size_t)xp * g.nya + (ra - g.ya_lo)) * nz + zq_lo;
-        for (int y = ra + lane; y <= rb; y += 32)
-            tma_load_1d(S + (y - (g.pad - H)) * SC + qcol0, src + (size_t)(y - ra) * nz,
-                        row_bytes, bar);
+        if (tma_box) {
+            const int row0 = (ga * g.Lp + xp) * g.nya - g.ya_lo;  // tensor row of y = 0
+            for (int k = lane; k < nbox; k += 32) {
+                const int ys = min(ra + k * kBoxRows, last);
+                tma_load_2d(S + (ys - (g.pad - H)) * SC, &tmA, z0 - HP, row0 + ys, bar);
+            }
+        } else {
+            const float *src = A + ((size_t)xp * g.nya + (ra - g.ya_lo)) * nz + zq_lo;
+            for (int y = ra + lane; y <= rb; y += 32)
+                tma_load_1d(S + (y - (g.pad - H)) * SC + qcol0, src + (size_t)(y - ra) * nz,
+                            row_bytes, bar);
+        }
     };
 
     int ra = 0, rb = -1, pra = 0, prb = -1;  // current and previous sampled rows
+    int fa = 0, fb = -1;                      // rows the attenuation copy wrote
     int xp = next_plane(x0, ra, rb);
-    if (use_tma && xp < x1) issue_tma(xp, ra, rb);
+    if (use_tma && xp < x1) issue_tma(xp, ra, rb, fa, fb);
     int parity = 0;
     unsigned phase = 0;
 #ifdef GB_PHASE_TIMING
@@ -230,7 +257,15 @@ __global__ void __launch_bounds__(TPB, 1)
         // the PSF); stale rows of the previous plane are cleared
         const float *Ap = A ? A + (size_t)xp * g.nya * nz : nullptr;
         if (VEC) {
+            // clear the sampled quads of rows outside [ra, rb]: the previous plane's rows
+            // and the rows the box copy wrote beyond the range
             for (int y = pra + warp; y <= prb; y += nwarp) {
+                if (y >= ra && y <= rb) continue;
+                float *Sr = S + (y - (g.pad - H)) * SC + qcol0;
+                for (int q = lane; q < nq; q += 32)
+                    *reinterpret_cast<float4 *>(Sr + 4 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            for (int y = fa + warp; y <= fb; y += nwarp) {
                 if (y >= ra && y <= rb) continue;
                 float *Sr = S + (y - (g.pad - H)) * SC + qcol0;
                 for (int q = lane; q < nq; q += 32)
@@ -290,10 +325,15 @@ __global__ void __launch_bounds__(TPB, 1)
                 S[(y - (g.pad - H)) * SC + c] = v;
             }
         }
-        __syncthreads();
         {
             long long t1 = GB_NOW();
             GB_T(1, t1 - t0);
+            t0 = t1;
+        }
+        __syncthreads();
+        {
+            long long t1 = GB_NOW();
+            GB_T(2, t1 - t0);
             t0 = t1;
         }
         // output rows (local y in [0, N)) that the blurred plane can reach
@@ -311,20 +351,23 @@ __global__ void __launch_bounds__(TPB, 1)
                 blur_first2<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
                                        nwarp);
         });
-        GB_T(6, rb - ra + 1);
-        GB_T(7, (b_hi - b_lo) * OB * tier_taps(K, tier));
+        {
+            long long t1 = GB_NOW();
+            GB_T(3, t1 - t0);
+            t0 = t1;
+        }
         __syncthreads();
         {
             long long t1 = GB_NOW();
-            GB_T(2, t1 - t0);
+            GB_T(4, t1 - t0);
             t0 = t1;
         }
         // S is free until the next phase 1: start the next plane's attenuation copy
         pra = ra;
         prb = rb;
-        int nra = 0, nrb = -1;
+        int nra = 0, nrb = -1, nfa = 0, nfb = -1;
         const int nxp = next_plane(xp + 1, nra, nrb);
-        if (use_tma && nxp < x1) issue_tma(nxp, nra, nrb);
+        if (use_tma && nxp < x1) issue_tma(nxp, nra, nrb, nfa, nfb);
         // phase 3: blur along z (2D PSF), optional attenuation after the PSF, accumulate
         {
             const int y_lo = b_lo * OB, y_hi = b_hi * OB;
@@ -407,20 +450,22 @@ __global__ void __launch_bounds__(TPB, 1)
         }
         {
             long long t1 = GB_NOW();
-            GB_T(3, t1 - t0);
-            GB_T(4, 1);
+            GB_T(5, t1 - t0);
+            GB_T(6, 1);
         }
         parity ^= 1;
         xp = nxp;
         ra = nra;
         rb = nrb;
+        fa = nfa;
+        fb = nfb;
     }
     if (failed) mbar_wait_bounded(bar, failed_phase, 1u << 16);
 #ifdef GB_PHASE_TIMING
-    if (g.phase && threadIdx.x == 0 && blockIdx.x * gridDim.y + blockIdx.y < 4096) {
-        tacc[5] = clock64() - t_start;
-        for (int k = 0; k < 8; k++)
-            g.phase[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
+    const int trow = (blockIdx.x * gridDim.y + blockIdx.y) * nwarp + warp;
+    if (g.phase && lane == 0 && trow < 4096) {
+        tacc[7] = clock64() - t_start;
+        for (int k = 0; k < 8; k++) g.phase[trow * 8 + k] = tacc[k];
     }
 #endif
     // partial ray sums of this item
@@ -451,6 +496,10 @@ inline bool fwd_fixed(int K, int N, int Zt, int tpb) {
     return (N + OB - 1) / OB * OB <= 128 && (Zt + OB - 1) / OB * OB <= 128;
 }
 
+// Tensor map of the attenuation table for the kernel's box copies (spect_fwd.cu); s_cols
+// is the kernel's S row length.  A zeroed map when the kernel makes no box copies.
+cudaError_t make_att_tmap(const SpectDev &g, int s_cols, CUtensorMap *out);
+
 template <int K, int TPB>
 inline cudaError_t launch_fwd_psf_t(const SpectDev &g, const float *f, const int *alist,
                                     const int4 *items, int n_items, int Zt, float *partials,
@@ -458,17 +507,22 @@ inline cudaError_t launch_fwd_psf_t(const SpectDev &g, const float *f, const int
     size_t smem = fwd_psf_smem_bytes(K, g.N, Zt, TPB);
     dim3 grid(n_items, (g.nz + Zt - 1) / Zt);
     const bool fx = fwd_fixed(K, g.N, Zt, TPB);
+    constexpr int HP = (K / 2 + 3) / 4 * 4, OB = (K <= 31) ? 8 : 4;
+    alignas(64) CUtensorMap tm;
+    cudaError_t e = make_att_tmap(
+        g, fx ? fwd_s_cols(128, HP) : fwd_s_cols((Zt + OB - 1) / OB * OB, HP), &tm);
+    if (e != cudaSuccess) return e;
     if (g.nz % 4 == 0) {
         if (fx)
-            k_fwd_psf<K, true, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
+            k_fwd_psf<K, true, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials, tm);
         else
-            k_fwd_psf<K, true, false, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
+            k_fwd_psf<K, true, false, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials, tm);
     } else {
         if (fx)
-            k_fwd_psf<K, false, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials);
+            k_fwd_psf<K, false, true, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt, partials, tm);
         else
             k_fwd_psf<K, false, false, TPB><<<grid, TPB, smem, st>>>(g, f, alist, items, Zt,
-                                                                    partials);
+                                                                    partials, tm);
     }
     return cudaGetLastError();
 }

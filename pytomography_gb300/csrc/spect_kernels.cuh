@@ -15,6 +15,7 @@
 // bilinearly with zero padding; the arithmetic below keeps the operation order of
 // the grid_sample CPU kernel (no FMA contraction) so the taps are reproducible.
 #pragma once
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -26,6 +27,7 @@ struct SpectDev {
     int *err;               // device error word (bounded waits that gave up), or null
     int2 *wrange;           // [G][Lp] W column range written per (slot, plane), or null
     int N, nz, pad, Lp;
+    int n_angles;
     int ya_lo, ya_hi, nya;  // stored row range of A and W
     float half;             // (Lp - 1) / 2
     const float *lin;       // [Lp]
@@ -250,6 +252,19 @@ __device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
             smem_u32(dst)),
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// 2-D TMA tensor copy global -> shared of one box of `map` at element coordinates (x, y)
+// (x innermost; x * 4 bytes a multiple of 16).  The box lands densely in shared memory
+// (128-byte aligned destination); elements outside the tensor read as zero.  Completion is
+// counted on `bar` (the full box bytes).
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
 }
 

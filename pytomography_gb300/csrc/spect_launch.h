@@ -18,7 +18,13 @@ inline int psf_bucket(int k) {
     return -1;
 }
 
-// tpb: threads per forward CTA, 512 (one CTA per SM) or 256 (two CTAs per SM)
+// Forward PSF kernel: rows per TMA box of its attenuation copy, and the length of its
+// sample rows in shared memory for a z slab of zw (rounded to the output block) with
+// half-halo hp: a multiple of 32 floats, so every row starts 128-byte aligned.
+constexpr int kBoxRows = 8;
+__host__ __device__ constexpr int fwd_s_cols(int zw, int hp) { return (zw + 2 * hp + 31) & ~31; }
+
+// tpb: threads per forward CTA, 512 or 768 (one CTA per SM)
 size_t fwd_psf_smem_bytes(int K, int N, int Zt, int tpb);
 size_t b1_psf_smem_bytes(int K, int N, int Zt);
 // Raise the dynamic shared-memory limit of the PSF kernels (done once at plan creation,

@@ -423,6 +423,7 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     p->H = psf ? K / 2 : 0;
     SpectDev &g = p->dev;
     g.N = p->N; g.nz = p->nz; g.pad = p->pad; g.Lp = p->Lp;
+    g.n_angles = p->n_angles;
     g.ya_lo = std::max(0, p->pad - p->H);
     g.ya_hi = std::min(p->Lp, p->pad + p->N + p->H);
     g.nya = g.ya_hi - g.ya_lo;
