@@ -22,12 +22,13 @@ namespace gb {
 static bool b1_fixed(int K, int N, int Zt);
 
 #ifdef GB_PHASE_TIMING
-// Per-CTA cycle counts of k_b1_psf (diagnostic builds only): [1] phase 1 (S load),
-// [2] y blur, [3] z blur + W store, [4] planes, [5] total, [6] rows, [7] rows x taps.
+// Per-warp cycle counts of k_b1_psf (diagnostic builds only), row CTA * warps + warp:
+// [1] phase 1 work (S load), [2] wait at the barrier after it, [3] y blur work, [4] wait
+// at the barrier after it, [5] z blur + W store work, [6] planes, [7] total.
 __device__ unsigned long long g_b1_phase_cycles[4096 * 8];
-#define GB_B1T(k, v)                            \
-    do {                                        \
-        if (threadIdx.x == 0) tacc[k] += (v);   \
+#define GB_B1T(k, v)                                  \
+    do {                                              \
+        if ((threadIdx.x & 31) == 0) tacc[k] += (v);  \
     } while (0)
 #define GB_B1NOW() clock64()
 #else
@@ -72,6 +73,28 @@ cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_ang
     return cudaGetLastError();
 }
 
+// OP consecutive floats (OP = 2 or 4, aligned to 4 * OP bytes) as one vector access
+template <int OP>
+__device__ __forceinline__ void ldg_vec(const float *p, float (&v)[OP]) {
+    if constexpr (OP == 4) {
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else {
+        static_assert(OP == 2, "vector of 2 or 4");
+        const float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+        v[0] = t.x; v[1] = t.y;
+    }
+}
+template <int OP>
+__device__ __forceinline__ void st_vec(float *p, const float (&v)[OP]) {
+    if constexpr (OP == 4) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+        static_assert(OP == 2, "vector of 2 or 4");
+        *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
+    }
+}
+
 // ---------------------------------------------------------------- B1 (PSF)
 // Grid (chunk of planes, angle slot, z slab).  Output rows o <-> padded y = pad-H+o,
 // o in [0, N+2H); input S rows i <-> padded y = pad-2H+i (projection rows at i in
@@ -94,7 +117,7 @@ __global__ void __launch_bounds__(512, 1)
     const int Z8 = (Zc + OB - 1) / OB * OB;
     constexpr int O8_FIX = (128 + 2 * H + OB - 1) / OB * OB;
     const int SC = FIXED ? 128 + 2 * H : Z8 + 2 * H, SR = O8 + 2 * H;  // S: [SR][SC]
-    const int TS = FIXED ? O8_FIX + 1 : O8 + 1, TR = Z8 + 2 * H;        // Tt: [TR][TS]
+    const int TS = FIXED ? O8_FIX + 2 : O8 + 2, TR = Z8 + 2 * H;        // Tt: [TR][TS], even
     extern __shared__ __align__(16) float sm[];
     float *S = sm;
     float *Tt = S + SR * SC;
@@ -151,98 +174,122 @@ __global__ void __launch_bounds__(512, 1)
                     P[(size_t)y * nz + z], Ap[(size_t)(g.pad + y - g.ya_lo) * nz + z]);
             }
         }
-        __syncthreads();
         {
             long long t1 = GB_B1NOW();
             GB_B1T(1, t1 - t0);
             t0 = t1;
         }
-        int tier = kTiers - 1;
-        if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : kTiers - 1;
-        tier_dispatch<K>(tier, [&](auto kk) {
-            constexpr int KK = decltype(kk)::value;
-            blur_first<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane, nwarp);
-        });
-        GB_B1T(6, rb - ra + 1);
-        GB_B1T(7, (rb - ra + 1) * tier_taps(K, tier));
         __syncthreads();
         {
             long long t1 = GB_B1NOW();
             GB_B1T(2, t1 - t0);
             t0 = t1;
         }
+        int tier = kTiers - 1;
+        if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : kTiers - 1;
+        // column pairs, blocks of OP = OB / 2 rows (as many warp-tasks as scalar blocks of OB)
+        constexpr int OP = OB / 2;
+        tier_dispatch<K>(tier, [&](auto kk) {
+            constexpr int KK = decltype(kk)::value;
+            blur_first2<K, KK, OP>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo * 2, b_hi * 2, warp,
+                                   lane, nwarp);
+        });
+        {
+            long long t1 = GB_B1NOW();
+            GB_B1T(3, t1 - t0);
+            t0 = t1;
+        }
+        __syncthreads();
+        {
+            long long t1 = GB_B1NOW();
+            GB_B1T(4, t1 - t0);
+            t0 = t1;
+        }
         {
             float *Wp = W + ((size_t)slot * g.Lp + xp) * g.nya * nz;
             const bool amul = Ap && g.att_first;
-            // warp-tasks (32-row chunk, z block); lanes take consecutive output rows
+            // warp-tasks (32-row chunk, two z blocks of OP): lanes 0-15 and 16-31 take the
+            // 16 row pairs of the chunk for z blocks 2q and 2q + 1
             const int nrc = ((b_hi - b_lo) * OB + 31) >> 5;
+            const int nzb = Z8 / OP, nzq = (nzb + 1) >> 1;
+            const int half = lane >> 4, pr = lane & 15;
             tier_dispatch<K>(tier, [&](auto kk) {
                 constexpr int KK = decltype(kk)::value;
                 float w[KK];
                 load_taps<K, KK>(tap + K, w);
-                for (int p = warp; p < nrc * (Z8 / OB); p += nwarp) {
-                    const int rc = p % nrc, zb = p / nrc;
-                    const int o_row = b_lo * OB + (rc << 5) + lane;
-                    if (o_row >= b_hi * OB) continue;
+                for (int p = warp; p < nrc * nzq; p += nwarp) {
+                    const int rc = p % nrc, zb = 2 * (p / nrc) + half;
+                    const int o_row = b_lo * OB + (rc << 5) + 2 * pr;  // rows o_row, o_row + 1
+                    if (o_row >= b_hi * OB || zb >= nzb) continue;
                     const int y = g.pad - H + o_row;
-                    const bool store = y >= ra && y <= rb;
-                    const int zl0 = zb * OB;
-                    const bool full = VEC && (zl0 + OB <= Zc);
+                    const bool st0 = y >= ra && y <= rb, st1 = y + 1 >= ra && y + 1 <= rb;
+                    const int zl0 = zb * OP;
+                    const bool full = VEC && (zl0 + OP <= Zc);
                     const size_t rowoff = (size_t)(y - g.ya_lo) * nz + z0 + zl0;
-                    float av[OB];
-                    if (store && amul) {  // issue the A loads before the blur arithmetic
-                        if (full) {
+                    float a0[OP], a1[OP];
+                    if (amul) {  // issue the A loads before the blur arithmetic
 #pragma unroll
-                            for (int j = 0; j < OB; j += 4) {
-                                const float4 a4 =
-                                    __ldg(reinterpret_cast<const float4 *>(Ap + rowoff + j));
-                                av[j] = a4.x;
-                                av[j + 1] = a4.y;
-                                av[j + 2] = a4.z;
-                                av[j + 3] = a4.w;
-                            }
+                        for (int j = 0; j < OP; j++) a0[j] = a1[j] = 0.f;
+                        if (full) {
+                            if (st0) ldg_vec<OP>(Ap + rowoff, a0);
+                            if (st1) ldg_vec<OP>(Ap + rowoff + nz, a1);
                         } else {
 #pragma unroll
-                            for (int j = 0; j < OB; j++) av[j] = zl0 + j < Zc ? Ap[rowoff + j] : 0.f;
+                            for (int j = 0; j < OP; j++) {
+                                if (zl0 + j >= Zc) continue;
+                                if (st0) a0[j] = Ap[rowoff + j];
+                                if (st1) a1[j] = Ap[rowoff + nz + j];
+                            }
                         }
                     }
-                    float o[OB];
+                    float2 o[OP];
                     if (g.psf2d) {
-                        blur_second<K, KK, OB>(Tt, w, TS, zb * OB, o_row, o);
+                        blur_second2<K, KK, OP, false>(Tt, w, TS, zl0, o_row, o);
                     } else {
 #pragma unroll
-                        for (int j = 0; j < OB; j++) o[j] = Tt[(zb * OB + j + H) * TS + o_row];
+                        for (int j = 0; j < OP; j++)
+                            o[j] = *reinterpret_cast<const float2 *>(Tt + (zl0 + j + H) * TS + o_row);
                     }
-                    if (!store) continue;
+                    if (!st0 && !st1) continue;
                     if (amul) {
 #pragma unroll
-                        for (int j = 0; j < OB; j++) o[j] = __fmul_rn(o[j], av[j]);
+                        for (int j = 0; j < OP; j++) {
+                            o[j].x = __fmul_rn(o[j].x, a0[j]);
+                            o[j].y = __fmul_rn(o[j].y, a1[j]);
+                        }
                     }
                     if (full) {
+                        float v0[OP], v1[OP];
 #pragma unroll
-                        for (int j = 0; j < OB; j += 4)
-                            *reinterpret_cast<float4 *>(Wp + rowoff + j) =
-                                make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);
+                        for (int j = 0; j < OP; j++) {
+                            v0[j] = o[j].x;
+                            v1[j] = o[j].y;
+                        }
+                        if (st0) st_vec<OP>(Wp + rowoff, v0);
+                        if (st1) st_vec<OP>(Wp + rowoff + nz, v1);
                     } else {
 #pragma unroll
-                        for (int j = 0; j < OB; j++)
-                            if (zl0 + j < Zc) Wp[rowoff + j] = o[j];
+                        for (int j = 0; j < OP; j++) {
+                            if (zl0 + j >= Zc) continue;
+                            if (st0) Wp[rowoff + j] = o[j].x;
+                            if (st1) Wp[rowoff + nz + j] = o[j].y;
+                        }
                     }
                 }
             });
         }
         {
             long long t1 = GB_B1NOW();
-            GB_B1T(3, t1 - t0);
-            GB_B1T(4, 1);
+            GB_B1T(5, t1 - t0);
+            GB_B1T(6, 1);
         }
         parity ^= 1;
     }
 #ifdef GB_PHASE_TIMING
-    if (threadIdx.x == 0 && blockIdx.x < 4096) {
-        tacc[5] = clock64() - t_start;
-        for (int k = 0; k < 8; k++)
-            g_b1_phase_cycles[(blockIdx.x * gridDim.y + blockIdx.y) * 8 + k] = tacc[k];
+    const int trow = (blockIdx.x * gridDim.y + blockIdx.y) * nwarp + warp;
+    if (lane == 0 && trow < 4096) {
+        tacc[7] = clock64() - t_start;
+        for (int k = 0; k < 8; k++) g_b1_phase_cycles[trow * 8 + k] = tacc[k];
     }
 #endif
 }
@@ -340,7 +387,7 @@ size_t b1_psf_smem_bytes(int K, int N, int Zt) {
     int Z8 = (Zt + OB - 1) / OB * OB;
     const bool fx = b1_fixed(K, N, Zt);
     size_t SC = fx ? 128 + 2 * H : Z8 + 2 * H;
-    size_t TS = fx ? (128 + 2 * H + OB - 1) / OB * OB + 1 : O8 + 1;
+    size_t TS = fx ? (128 + 2 * H + OB - 1) / OB * OB + 2 : O8 + 2;  // even: float2 pairs
     return sizeof(float) * ((size_t)(O8 + 2 * H) * SC + (size_t)(Z8 + 2 * H) * TS + 4 * K);
 }
 
