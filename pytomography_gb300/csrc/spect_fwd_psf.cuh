@@ -271,9 +271,10 @@ __global__ void __launch_bounds__(TPB, 1)
                 for (int q = lane; q < nq; q += 32)
                     *reinterpret_cast<float4 *>(Sr + 4 * q) = make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            // RB consecutive rows per warp and batch (4 with 512 threads, 2 with 768):
-            // neighbouring rows share about half of their bilinear taps, which then hit in L1
-            constexpr int RB = TAPS_SMEM ? 2 : 4;
+            // RB = 2 consecutive rows per warp and batch: neighbouring rows share about half
+            // of their bilinear taps, which then hit in L1.  (Four rows per batch keep more
+            // loads in flight but leave too few registers for the blur passes: slower.)
+            constexpr int RB = 2;
             for (int y0 = ra + RB * warp; y0 <= rb; y0 += RB * nwarp) {
                 int ys[RB];
                 bool okr[RB];
