@@ -210,6 +210,47 @@ __device__ __forceinline__ void blur_first2(const float *__restrict__ S, float *
     }
 }
 
+// blur_first2 reading each tap from shared memory (a broadcast load) inside the tap loop
+// instead of holding all taps in registers.
+template <int K, int KK, int OB>
+__device__ __forceinline__ void blur_first2_st(const float *__restrict__ S,
+                                               float *__restrict__ Tt,
+                                               const float *__restrict__ tap, int SC, int TS,
+                                               int c_lo, int c_hi, int b_lo, int b_hi, int warp,
+                                               int lane, int nwarp) {
+    static_assert(OB % 2 == 0, "pair stores need an even row block");
+    constexpr int OFF = (K - KK) / 2;
+    const int c0 = c_lo & ~1, c1 = (c_hi + 1) & ~1;
+    const int nb = b_hi - b_lo;
+    const int ncc = (c1 - c0 + 63) >> 6;
+    const int SC2 = SC >> 1;
+    for (int p = warp; p < ncc * nb; p += nwarp) {
+        const int cc = p % ncc, yb = b_lo + p / ncc;
+        const int c = c0 + (cc << 6) + 2 * lane;
+        if (c >= c1) continue;
+        const float2 *sp = reinterpret_cast<const float2 *>(S + (yb * OB + OFF) * SC + c);
+        float2 win[OB + KK - 1];
+#pragma unroll
+        for (int i = 0; i < OB + KK - 1; i++) win[i] = sp[i * SC2];
+        float2 o[OB];
+#pragma unroll
+        for (int j = 0; j < OB; j++) o[j] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < KK; t++) {
+            const float wv = tap[OFF + t];
+            const float2 wt = make_float2(wv, wv);
+#pragma unroll
+            for (int j = 0; j < OB; j++) o[j] = __ffma2_rn(wt, win[j + t], o[j]);
+        }
+        float *tq = Tt + c * TS + yb * OB;
+#pragma unroll
+        for (int j = 0; j < OB; j += 2) {
+            *reinterpret_cast<float2 *>(tq + j) = make_float2(o[j].x, o[j + 1].x);
+            *reinterpret_cast<float2 *>(tq + TS + j) = make_float2(o[j].y, o[j + 1].y);
+        }
+    }
+}
+
 // Second pass of one task over the column pair (col, col + 1), col even; ACC: o += blur.
 template <int K, int KK, int OB, bool ACC>
 __device__ __forceinline__ void blur_second2(const float *__restrict__ Tt,

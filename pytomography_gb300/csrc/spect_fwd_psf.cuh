@@ -340,7 +340,8 @@ __global__ void __launch_bounds__(TPB, 1)
         // output rows (local y in [0, N)) that the blurred plane can reach
         const int o_lo = max(0, ra - H - g.pad), o_hi = min(N, rb + H - g.pad + 1);
         const int b_lo = o_lo / OB, b_hi = (o_hi + OB - 1) / OB;
-        // phase 2: blur along y, write transposed (tap tier of the plane)
+        // phase 2: blur along y, write transposed (tap tier of the plane; taps read from
+        // shared memory, which leaves the registers to the packed windows)
         int tier = kTiers - 1;
         if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : kTiers - 1;
         tier_dispatch<K>(tier, [&](auto kk) {
@@ -349,8 +350,8 @@ __global__ void __launch_bounds__(TPB, 1)
                 blur_first_st<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
                                          nwarp);
             else
-                blur_first2<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
-                                       nwarp);
+                blur_first2_st<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp,
+                                          lane, nwarp);
         });
         {
             long long t1 = GB_NOW();
