@@ -24,8 +24,9 @@ static bool b1_fixed(int K, int N, int Zt);
 #ifdef GB_PHASE_TIMING
 // Per-warp cycle counts of k_b1_psf (diagnostic builds only), row CTA * warps + warp:
 // [1] phase 1 work (S load), [2] wait at the barrier after it, [3] y blur work, [4] wait
-// at the barrier after it, [5] z blur + W store work, [6] planes, [7] total.
-__device__ unsigned long long g_b1_phase_cycles[4096 * 8];
+// at the barrier after it, [5] z blur + W store work, [6] planes, [7] total, [8] rows,
+// [9] rows x taps, [10] planes of the work item.
+__device__ unsigned long long g_b1_phase_cycles[4096 * 16];
 #define GB_B1T(k, v)                                  \
     do {                                              \
         if ((threadIdx.x & 31) == 0) tacc[k] += (v);  \
@@ -144,8 +145,9 @@ __global__ void __launch_bounds__(512, 1)
     int2 *wr = g.wrange + (size_t)slot * g.Lp;
     int parity = 0;
 #ifdef GB_PHASE_TIMING
-    unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long tacc[16] = {};
     const long long t_start = clock64();
+    tacc[10] = x1 - x0;
 #endif
     long long t0 = GB_B1NOW();
     for (int xp = x0; xp < x1; ++xp) {
@@ -194,6 +196,8 @@ __global__ void __launch_bounds__(512, 1)
             blur_first2<K, KK, OP>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo * 2, b_hi * 2, warp,
                                    lane, nwarp);
         });
+        GB_B1T(8, rb - ra + 1);
+        GB_B1T(9, (rb - ra + 1) * tier_taps(K, tier));
         {
             long long t1 = GB_B1NOW();
             GB_B1T(3, t1 - t0);
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(512, 1)
     const int trow = (blockIdx.x * gridDim.y + blockIdx.y) * nwarp + warp;
     if (lane == 0 && trow < 4096) {
         tacc[7] = clock64() - t_start;
-        for (int k = 0; k < 8; k++) g_b1_phase_cycles[trow * 8 + k] = tacc[k];
+        for (int k = 0; k < 16; k++) g_b1_phase_cycles[trow * 16 + k] = tacc[k];
     }
 #endif
 }
@@ -299,7 +303,7 @@ extern "C" int gb_debug_b1_phase_cycles(unsigned long long *out, int n) {
     return (int)cudaMemcpyFromSymbol(out, g_b1_phase_cycles, sizeof(unsigned long long) * (size_t)n);
 }
 extern "C" int gb_debug_b1_phase_reset(void) {
-    static unsigned long long zero[4096 * 8];
+    static unsigned long long zero[4096 * 16];
     return (int)cudaMemcpyToSymbol(g_b1_phase_cycles, zero, sizeof(zero));
 }
 #endif

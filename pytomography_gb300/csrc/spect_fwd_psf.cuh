@@ -21,10 +21,11 @@ namespace gb {
 
 #ifdef GB_PHASE_TIMING
 // Per-warp cycle counts of the forward kernel's phases (diagnostic builds only, written to
-// g.phase[(CTA * warps + warp) * 8 + k] when set): [0] waits for the attenuation copy,
+// g.phase[(CTA * warps + warp) * 16 + k] when set): [0] waits for the attenuation copy,
 // [1] phase 1 work, [2] wait at the barrier after phase 1, [3] phase 2 work, [4] wait at
 // the barrier after phase 2, [5] phase 3 work (with the next plane's copy issue),
-// [6] planes processed, [7] total.
+// [6] planes processed, [7] total, [8] rows sampled, [9] output rows x taps, [10] planes
+// of the work item.
 #define GB_T(k, v)                                              \
     do {                                                        \
         if ((threadIdx.x & 31) == 0) tacc[k] += (v);            \
@@ -225,8 +226,9 @@ __global__ void __launch_bounds__(TPB, 1)
     int parity = 0;
     unsigned phase = 0;
 #ifdef GB_PHASE_TIMING
-    unsigned long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long tacc[16] = {};
     const long long t_start = clock64();
+    tacc[10] = x1 - x0;
 #endif
     long long t0 = GB_NOW();
     while (xp < x1) {
@@ -353,6 +355,8 @@ __global__ void __launch_bounds__(TPB, 1)
                 blur_first2_st<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp,
                                           lane, nwarp);
         });
+        GB_T(8, rb - ra + 1);
+        GB_T(9, (b_hi - b_lo) * OB * tier_taps(K, tier));
         {
             long long t1 = GB_NOW();
             GB_T(3, t1 - t0);
@@ -467,7 +471,7 @@ __global__ void __launch_bounds__(TPB, 1)
     const int trow = (blockIdx.x * gridDim.y + blockIdx.y) * nwarp + warp;
     if (g.phase && lane == 0 && trow < 4096) {
         tacc[7] = clock64() - t_start;
-        for (int k = 0; k < 8; k++) g.phase[trow * 8 + k] = tacc[k];
+        for (int k = 0; k < 16; k++) g.phase[trow * 16 + k] = tacc[k];
     }
 #endif
     // partial ray sums of this item

@@ -132,14 +132,16 @@ static bool host_plane_rows(const gb_spect_plan *p, int a, int xp, int ylo, int 
 }
 
 // Estimated cost (SM cycles) of every plane of angle a, a linear model fitted to
-// per-CTA cycle counts of both kernels on GB300 over object sizes 64-128 and 60-120
-// angles: a fixed cost per occupied plane (barriers, pipeline drain), a cost per sampled
-// row and a cost per blurred output row and tap (the plane's tap tier sets the taps).
-//   forward: 6100 + 158 rows + 4.4 (output rows x taps)
-//   B1:      3700 + 113 rows + 2.5 (rows x taps)
-// A plane that no sample reaches costs about one plane-support test.
+// per-CTA cycle counts of both kernels on GB300 (object sizes 64-128, 60-120 angles,
+// three subsets each): a fixed cost per occupied plane (barriers, pipeline drain), a cost
+// per sampled row and a cost per blurred output row and tap (the plane's tap tier sets
+// the taps).
+//   forward: 6360 + 106 rows + 2.76 (output rows x taps); a plane no sample reaches: 100
+//   B1:      4470 +  97 rows + 2.64 (rows x taps);        a plane no sample reaches: 600
+// (The forward skips empty planes with a support test; B1 also records their empty row
+// range.)
 static std::vector<double> plane_work(const gb_spect_plan *p, int a, bool fwd) {
-    std::vector<double> w(p->Lp, 200.0);
+    std::vector<double> w(p->Lp, fwd ? 100.0 : 600.0);
     const int H = p->H, K = p->dev.K;
     const int ylo = std::max(0, p->pad - H), yhi = std::min(p->Lp, p->pad + p->N + H);
     const int grp = p->h_group.empty() ? 0 : p->h_group[a];
@@ -151,9 +153,9 @@ static std::vector<double> plane_work(const gb_spect_plan *p, int a, bool fwd) {
         const double rows = rb - ra + 1;
         if (fwd) {
             const int o = std::min(p->N, rb + H - p->pad + 1) - std::max(0, ra - H - p->pad);
-            w[xp] = 6100.0 + 158.0 * rows + 4.4 * kk * std::max(0, o);
+            w[xp] = 6360.0 + 106.0 * rows + 2.76 * kk * std::max(0, o);
         } else {
-            w[xp] = 3700.0 + 113.0 * rows + 2.5 * kk * rows;
+            w[xp] = 4470.0 + 97.0 * rows + 2.64 * kk * rows;
         }
     }
     return w;
@@ -916,8 +918,8 @@ gb_status gb_rdp_gradient(const float *f, float *grad, int32_t nx, int32_t ny, i
 }
 
 #ifdef GB_PHASE_TIMING
-// Diagnostic builds: per-CTA phase cycle counts of the plan's forward launches ([4096][8],
-// layout in spect_fwd_psf.cuh), attached on first use.
+// Diagnostic builds: per-warp phase cycle counts of the plan's forward launches
+// ([4096][16], layout in spect_fwd_psf.cuh), attached on first use.
 extern "C" int gb_debug_fwd_phase_cycles(gb_spect_plan *p, unsigned long long *out, int n) {
     if (!p->dev.phase) return -1;
     return (int)cudaMemcpy(out, p->dev.phase, sizeof(unsigned long long) * (size_t)n,
@@ -925,10 +927,10 @@ extern "C" int gb_debug_fwd_phase_cycles(gb_spect_plan *p, unsigned long long *o
 }
 extern "C" int gb_debug_fwd_phase_reset(gb_spect_plan *p) {
     if (!p->dev.phase) {
-        cudaError_t e = cudaMalloc(&p->dev.phase, sizeof(unsigned long long) * 4096 * 8);
+        cudaError_t e = cudaMalloc(&p->dev.phase, sizeof(unsigned long long) * 4096 * 16);
         if (e != cudaSuccess) return (int)e;
     }
-    return (int)cudaMemset(p->dev.phase, 0, sizeof(unsigned long long) * 4096 * 8);
+    return (int)cudaMemset(p->dev.phase, 0, sizeof(unsigned long long) * 4096 * 16);
 }
 #endif
 
