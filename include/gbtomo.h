@@ -222,7 +222,8 @@ gb_status gb_pet_set_subsets(gb_pet_plan *plan, int32_t n_subsets);
 gb_status gb_pet_forward(gb_pet_plan *plan, const float *img, float *proj, int32_t subset,
                          gb_stream_t stream);
 /* Adjoint: image (overwritten) = H_m^T proj.  Replaces joseph3d_back_tof_lm /
- * joseph3d_back in PETLMSystemMatrix.backward (petlm_system_matrix.py:299-363). */
+ * joseph3d_back in PETLMSystemMatrix.backward (petlm_system_matrix.py:299-363).
+ * img must be 16-byte aligned (vector atomics). */
 gb_status gb_pet_backward(gb_pet_plan *plan, const float *proj, float *img, int32_t subset,
                           gb_stream_t stream);
 /* Non-TOF line integrals of `img` along the subset's events (attenuation path,
@@ -231,7 +232,8 @@ gb_status gb_pet_lor_forward(gb_pet_plan *plan, const float *img, float *proj, i
                              int32_t use_tof, gb_stream_t stream);
 /* Sensitivity image: non-TOF back projection of (weights * exp(-H mu) + add) over the
  * LOR set `pairs` [n_pairs][2] (device), or over every crystal pair i < j when pairs is
- * NULL (petlm_system_matrix.py:112-174).  weights / mu may be NULL. */
+ * NULL (petlm_system_matrix.py:112-174).  weights / mu may be NULL; img must be 16-byte
+ * aligned. */
 gb_status gb_pet_sensitivity(gb_pet_plan *plan, const int32_t *pairs, int64_t n_pairs,
                              const float *weights, const float *mu, float add, float *img,
                              gb_stream_t stream);
@@ -276,7 +278,8 @@ int32_t gb_pet_sino_subset_size(const gb_pet_sino_plan *plan, int32_t subset);
 gb_status gb_pet_sino_forward(gb_pet_sino_plan *plan, const float *img, float *proj,
                               int32_t subset, int32_t use_tof, gb_stream_t stream);
 /* img = H^T proj (overwrites img): joseph3d_back / joseph3d_back_tof_sino (:263-292);
- * use_tof = 0 on a TOF plan is the reference's force_nonTOF. */
+ * use_tof = 0 on a TOF plan is the reference's force_nonTOF.  img must be 16-byte
+ * aligned. */
 gb_status gb_pet_sino_backward(gb_pet_sino_plan *plan, const float *proj, float *img,
                                int32_t subset, int32_t use_tof, gb_stream_t stream);
 /* prob [n_sel][n_radial][n_planes] = exp(-H mu), the attenuation probability sinogram

@@ -276,6 +276,7 @@ gb_status gb_pet_plan_create(const gb_pet_desc *d, gb_pet_plan **out) {
     auto *p = new gb_pet_plan();
     PetDev &g = p->dev;
     g.n[0] = d->nx; g.n[1] = d->ny; g.n[2] = d->nz;
+    g.n_vox = d->nx * d->ny * d->nz;
     g.vox[0] = d->vx; g.vox[1] = d->vy; g.vox[2] = d->vz;
     g.org[0] = d->ox; g.org[1] = d->oy; g.org[2] = d->oz;
     g.n_det = d->n_det;
@@ -386,6 +387,7 @@ gb_status gb_pet_backward(gb_pet_plan *p, const float *proj, float *img, int32_t
                           gb_stream_t stream) {
     clear_error();
     GB_CHECK_ARG(p && img && proj, "null argument");
+    GB_CHECK_ARG(((uintptr_t)img & 15) == 0, "image buffer must be 16-byte aligned");
     GB_CHECK_ARG(subset < p->n_subsets, "subset out of range");
     long long first, stride, n;
     subset_range(p, subset, first, stride, n);
@@ -445,6 +447,7 @@ gb_status gb_pet_sensitivity(gb_pet_plan *p, const int32_t *pairs, int64_t n_pai
                              gb_stream_t stream) {
     clear_error();
     GB_CHECK_ARG(p && img, "null argument");
+    GB_CHECK_ARG(((uintptr_t)img & 15) == 0, "image buffer must be 16-byte aligned");
     long long total = (long long)p->dev.n_det * (p->dev.n_det - 1) / 2;
     if (!pairs) n_pairs = total;
     GB_CHECK_ARG(n_pairs >= 0, "negative pair count");

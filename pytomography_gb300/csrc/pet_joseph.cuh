@@ -37,6 +37,7 @@ inline void tof_weight_table(float bw, float sigma, float n_sigmas, std::vector<
 
 struct PetDev {
     int n[3];
+    int n_vox;  // n[0] * n[1] * n[2]
     float vox[3], org[3];
     const float *lut;  // [n_det][3]
     int n_det;
@@ -56,7 +57,8 @@ __device__ __forceinline__ int pick(int a, int b, int c, int k) {
 
 // Joseph trace of one LOR.  BACK = false: returns sum of weighted samples of cimg.
 // BACK = true: adds val * weights into img (atomics; the two corners of a bilinear pair
-// that are neighbours in z go out as one 8-byte vector atomic when aligned).
+// that are neighbours in z go out as one 16-byte vector atomic, zeros in the other two
+// lanes, when they share an aligned quad inside the image: 3 pairs in 4).
 // Along the principal axis k the plane parameter t, the sample coordinates on the two
 // other axes (in voxel units) and the TOF distance s are linear in the plane index i and
 // are evaluated as base + i * step.  Axis-dependent quantities are selected into
@@ -150,8 +152,21 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
                 const float wr = val * w * (q ? wo : 1.f - wo);
                 const float v0 = wr * (1.f - wz), v1 = wr * wz;
                 const int off = base + r * so + jz;
-                if (ok0 && ok1 && (off & 1) == 0) {
-                    atomicAdd(reinterpret_cast<float2 *>(img + off), make_float2(v0, v1));
+                const int qd = off & 3;  // the pair's position in its aligned quad
+                if (ok0 && ok1 && qd < 3 && off - qd + 4 <= g.n_vox) {
+                    // both corners in one 16-byte quad: one vector atomic (zeros elsewhere)
+                    float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (qd == 0) {
+                        v4.x = v0;
+                        v4.y = v1;
+                    } else if (qd == 1) {
+                        v4.y = v0;
+                        v4.z = v1;
+                    } else {
+                        v4.z = v0;
+                        v4.w = v1;
+                    }
+                    atomicAdd(reinterpret_cast<float4 *>(img + (off - qd)), v4);
                 } else {
                     if (ok0) atomicAdd(img + off, v0);
                     if (ok1) atomicAdd(img + off + 1, v1);

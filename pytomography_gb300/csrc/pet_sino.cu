@@ -160,6 +160,7 @@ gb_status gb_pet_sino_plan_create(const gb_pet_sino_desc *d, gb_pet_sino_plan **
     auto *p = new gb_pet_sino_plan();
     PetDev &g = p->dev;
     g.n[0] = d->nx; g.n[1] = d->ny; g.n[2] = d->nz;
+    g.n_vox = d->nx * d->ny * d->nz;
     g.vox[0] = d->vx; g.vox[1] = d->vy; g.vox[2] = d->vz;
     g.org[0] = d->ox; g.org[1] = d->oy; g.org[2] = d->oz;
     g.tof = d->tof;
@@ -254,6 +255,7 @@ gb_status gb_pet_sino_backward(gb_pet_sino_plan *p, const float *proj, float *im
                                int32_t subset, int32_t use_tof, gb_stream_t stream) {
     clear_error();
     GB_CHECK_ARG(p && img && proj, "null argument");
+    GB_CHECK_ARG(((uintptr_t)img & 15) == 0, "image buffer must be 16-byte aligned");
     GB_CHECK_ARG(subset < p->n_subsets, "subset out of range");
     int first, stride, n;
     sino_range(p, subset, first, stride, n);
