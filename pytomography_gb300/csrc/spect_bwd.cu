@@ -44,11 +44,18 @@ __device__ unsigned long long g_b1_phase_cycles[4096 * 16];
 // A[a][xp][y][z] = exp(-(sum_{k>=xp} mu_rot[k]*dx - mu_rot[xp]*dx/2)) for the stored
 // rows y in [ya_lo, ya_hi); mu_rot uses the forward rotation of angle a.
 // (get_prob_of_detection_matrix, attenuation.py:11-21; rev_cumsum, utils/misc.py:8-19)
-__global__ void k_atten(SpectDev g, const float *__restrict__ mu, float dx, float *__restrict__ A) {
+// The samples of PU planes are gathered before their running sums (same order of
+// additions as one plane at a time), so PU planes' loads are in flight together.
+template <bool VEC>
+__global__ void __launch_bounds__(256)
+    k_atten(SpectDev g, const float *__restrict__ mu, float dx, float *__restrict__ A) {
+    constexpr int W = VEC ? 4 : 1;       // z values per thread
+    constexpr int PU = VEC ? 4 : 8;      // planes sampled per step
     const int a = blockIdx.y;
+    const int nzw = g.nz / W;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.nya * g.nz) return;
-    const int r = i / g.nz, z = i % g.nz;
+    if (i >= g.nya * nzw) return;
+    const int r = i / nzw, z = (i % nzw) * W;
     const int y = g.ya_lo + r;
     float th[6];
 #pragma unroll
@@ -56,21 +63,56 @@ __global__ void k_atten(SpectDev g, const float *__restrict__ mu, float dx, floa
     const float lc = g.lin[y];
     float *out = A + (size_t)a * g.Lp * g.nya * g.nz + (size_t)r * g.nz + z;
     const size_t plane = (size_t)g.nya * g.nz;
-    float run = 0.f;
-    for (int xp = g.Lp - 1; xp >= 0; --xp) {
-        float ix, iy;
-        rot_coords(th, g.lin[xp], lc, g.half, ix, iy);
-        Bilin b = bilin(ix, iy);
-        float v = __fmul_rn(sample(mu, g.N, g.N, g.nz, g.pad, g.pad, b, z), dx);
-        run = __fadd_rn(run, v);
-        out[(size_t)xp * plane] = expf(-__fsub_rn(run, __fmul_rn(v, 0.5f)));
+    float run[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) run[w] = 0.f;
+    for (int x0 = g.Lp - 1; x0 >= 0; x0 -= PU) {
+        float v[PU][W];
+#pragma unroll
+        for (int u = 0; u < PU; u++) {
+            const int xp = max(x0 - u, 0);
+            float ix, iy;
+            rot_coords(th, g.lin[xp], lc, g.half, ix, iy);
+            const Bilin b = bilin(ix, iy);
+            if constexpr (VEC) {
+                float4 s4;
+                sample4(mu, g.N, g.N, g.nz, g.pad, g.pad, b, z, s4);
+                v[u][0] = __fmul_rn(s4.x, dx);
+                v[u][1] = __fmul_rn(s4.y, dx);
+                v[u][2] = __fmul_rn(s4.z, dx);
+                v[u][3] = __fmul_rn(s4.w, dx);
+            } else {
+                v[u][0] = __fmul_rn(sample(mu, g.N, g.N, g.nz, g.pad, g.pad, b, z), dx);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < PU; u++) {
+            const int xp = x0 - u;
+            if (xp < 0) break;
+            float e[W];
+#pragma unroll
+            for (int w = 0; w < W; w++) {
+                run[w] = __fadd_rn(run[w], v[u][w]);
+                e[w] = expf(-__fsub_rn(run[w], __fmul_rn(v[u][w], 0.5f)));
+            }
+            if constexpr (VEC)
+                *reinterpret_cast<float4 *>(out + (size_t)xp * plane) =
+                    make_float4(e[0], e[1], e[2], e[3]);
+            else
+                out[(size_t)xp * plane] = e[0];
+        }
     }
 }
 
 cudaError_t launch_atten(const SpectDev &g, const float *mu, float dx, int n_angles, float *A,
                          cudaStream_t st) {
-    dim3 grid((g.nya * g.nz + 255) / 256, n_angles);
-    k_atten<<<grid, 256, 0, st>>>(g, mu, dx, A);
+    if (g.nz % 4 == 0) {
+        dim3 grid((g.nya * (g.nz / 4) + 255) / 256, n_angles);
+        k_atten<true><<<grid, 256, 0, st>>>(g, mu, dx, A);
+    } else {
+        dim3 grid((g.nya * g.nz + 255) / 256, n_angles);
+        k_atten<false><<<grid, 256, 0, st>>>(g, mu, dx, A);
+    }
     return cudaGetLastError();
 }
 
