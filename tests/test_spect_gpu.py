@@ -118,6 +118,8 @@ def _synthetic(n, nz, n_angles, seed, att=True):
     (128, 128, 120, "ap", 22.0, 0.442),  # the 128^3 / 120-angle att+PSF geometry (one subset)
     (37, 21, 9, "pa", 18.0, 0.5),        # odd sizes, PSF before attenuation
     (20, 1, 5, "ap", 15.0, 0.6),         # a single slice
+    (144, 40, 6, "ap", 35.0, 0.442),     # rows beyond 128: run-time shared-memory strides
+    (64, 256, 2, "ap", 22.0, 0.442),     # a z slab wider than a tensor box: 1-D row copies
 ])
 def test_full_size_geometries_vs_oracle(n, nz, n_angles, order, radius, dr, cuda):
     from pytomography_gb300.metadata.SPECT import SPECTObjectMeta, SPECTProjMeta, SPECTPSFMeta
