@@ -98,6 +98,26 @@ def test_pet_forward_backward_vs_oracle(tof, cuda):
 
 
 @pytest.mark.gpu
+def test_pet_backward_odd_image_and_alignment(cuda):
+    """An image whose voxel count is not a multiple of 4 (the 16-byte vector atomics stop
+    at the image end), and the C entry point's 16-byte alignment check of the image."""
+    from pytomography_gb300 import _lib
+    shape = (15, 13, 7)
+    H, o, ev, img = _setup(True, shape=shape, vox=(8.0, 8.0, 8.0))
+    p = np.random.default_rng(5).random(len(ev))
+    pt = torch.tensor(p, dtype=torch.float32, device=cuda)
+    bwd = H.backward(pt).cpu().numpy()
+    ref = o.backward(p, ev)
+    assert np.abs(ref).sum() > 0
+    assert rel_l2(bwd, ref) < TOL
+    buf = torch.zeros(int(np.prod(shape)) + 4, device=cuda)
+    rc = H._lib.gb_pet_backward(H._plan, _lib.ptr(pt), buf.data_ptr() + 4, -1,
+                                _lib.stream_handle(cuda))
+    assert rc != 0  # rejected on the host: nothing launched
+    assert float(buf.abs().sum()) == 0.0
+
+
+@pytest.mark.gpu
 def test_pet_adjoint_dot(cuda):
     H, o, ev, img = _setup(True, n_events=5000, seed=3)
     f = torch.tensor(img, dtype=torch.float64, device=cuda)
