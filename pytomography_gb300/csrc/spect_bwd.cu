@@ -674,19 +674,35 @@ cudaError_t launch_b2_gather(const SpectDev &g, const float *W, const int *alist
 
 // ------------------------------------------------------------ B2 scatter
 // Exact adjoint of the forward rotation: every W element is scattered to the four
-// object voxels the forward sample at the same position gathered from.
+// object voxels the forward sample at the same position gathered from.  VEC: a thread
+// takes a z quad and each corner gets one 16-byte vector atomic (nz % 4 == 0, out 16-byte
+// aligned); the per-element products are the same as one element at a time.
+template <bool VEC>
 __global__ void __launch_bounds__(256)
     k_b2_scatter(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
                  float *__restrict__ out) {
+    constexpr int V = VEC ? 4 : 1;
     const int slot = blockIdx.z, xp = blockIdx.y;
+    const int nzv = g.nz / V;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.nya * g.nz) return;
-    const int r = i / g.nz, z = i % g.nz;
+    if (i >= g.nya * nzv) return;
+    const int r = i / nzv, z = (i % nzv) * V;
     const int yp = g.ya_lo + r;
     const int2 rg = g.wrange[(size_t)slot * g.Lp + xp];
     if (r < rg.x || r >= rg.y) return;
-    const float v = W[(((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z];
-    if (v == 0.f) return;
+    const float *wp = W + (((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z;
+    float v[V];
+    if constexpr (VEC) {
+        const float4 t = *reinterpret_cast<const float4 *>(wp);
+        v[0] = t.x;
+        v[1] = t.y;
+        v[2] = t.z;
+        v[3] = t.w;
+        if (t.x == 0.f && t.y == 0.f && t.z == 0.f && t.w == 0.f) return;
+    } else {
+        v[0] = *wp;
+        if (v[0] == 0.f) return;
+    }
     const float *th = g.theta_fwd + 6 * alist[slot];
     float ix, iy;
     rot_coords(th, g.lin[xp], g.lin[yp], g.half, ix, iy);
@@ -697,15 +713,26 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         int rr = r0 + (q >> 1), cc = c0 + (q & 1);
-        if ((unsigned)rr < (unsigned)N && (unsigned)cc < (unsigned)N)
-            atomicAdd(out + ((size_t)rr * N + cc) * nz + z, __fmul_rn(wt[q], v));
+        if ((unsigned)rr >= (unsigned)N || (unsigned)cc >= (unsigned)N) continue;
+        float *o = out + ((size_t)rr * N + cc) * nz + z;
+        if constexpr (VEC)
+            atomicAdd(reinterpret_cast<float4 *>(o),
+                      make_float4(__fmul_rn(wt[q], v[0]), __fmul_rn(wt[q], v[1]),
+                                  __fmul_rn(wt[q], v[2]), __fmul_rn(wt[q], v[3])));
+        else
+            atomicAdd(o, __fmul_rn(wt[q], v[0]));
     }
 }
 
 cudaError_t launch_b2_scatter(const SpectDev &g, const float *W, const int *alist, int n_slots,
                               float *out, cudaStream_t st) {
-    dim3 grid((g.nya * g.nz + 255) / 256, g.Lp, n_slots);
-    k_b2_scatter<<<grid, 256, 0, st>>>(g, W, alist, out);
+    if (g.nz % 4 == 0 && ((uintptr_t)out & 15) == 0) {
+        dim3 grid((g.nya * (g.nz / 4) + 255) / 256, g.Lp, n_slots);
+        k_b2_scatter<true><<<grid, 256, 0, st>>>(g, W, alist, out);
+    } else {
+        dim3 grid((g.nya * g.nz + 255) / 256, g.Lp, n_slots);
+        k_b2_scatter<false><<<grid, 256, 0, st>>>(g, W, alist, out);
+    }
     return cudaGetLastError();
 }
 
