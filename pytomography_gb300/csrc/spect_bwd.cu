@@ -490,6 +490,49 @@ __device__ __forceinline__ float rdp_sum(const float *__restrict__ f, int nx, in
     return acc;
 }
 
+// rdp_sum for the four voxels z..z+3 of a z quad (z % 4 == 0, nz % 4 == 0), used by the
+// fused BSREM step: each (x, y) neighbour row is loaded once (z-1, the quad, z+4,
+// clamped), every voxel adds its 26 terms in rdp_sum's order, and the term arithmetic
+// uses FMAs and the fast division (about 2 ulp; exact division for denominators below
+// 2^-100, where the fast reciprocal would overflow).  The result differs from rdp_sum by
+// rounding only (well inside the 1e-5 agreement with the reference).
+__device__ __forceinline__ void rdp_sum4(const float *__restrict__ f, int nx, int ny, int nz,
+                                         int x, int y, int z, const float (&fr)[4],
+                                         const UpdateArgs &u, float (&acc)[4]) {
+#pragma unroll
+    for (int v = 0; v < 4; v++) acc[v] = 0.f;
+    int n = 0;
+    const float two_d = 2.f * u.rdelta;
+#pragma unroll
+    for (int i = -1; i <= 1; i++) {
+        const int xi = min(max(x + i, 0), nx - 1);
+#pragma unroll
+        for (int j = -1; j <= 1; j++) {
+            const int yj = min(max(y + j, 0), ny - 1);
+            const float *p = f + ((size_t)xi * ny + yj) * nz;
+            const float4 c = __ldg(reinterpret_cast<const float4 *>(p + z));
+            const float row[6] = {__ldg(p + max(z - 1, 0)), c.x, c.y, c.z, c.w,
+                                  __ldg(p + min(z + 4, nz - 1))};
+#pragma unroll
+            for (int k = -1; k <= 1; k++) {
+                if (i == 0 && j == 0 && k == 0) continue;
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const float fs = row[1 + v + k], r = fr[v];
+                    const float d = r - fs, ad = fabsf(d);
+                    const float num = d * (fmaf(u.gamma, ad, fmaf(3.f, fs, r)) + two_d);
+                    const float den = fmaf(u.gamma, ad, r + fs) + u.rdelta;
+                    const float den2 = den * den;
+                    const float phi =
+                        den2 > 7.8886e-31f ? __fdividef(num, den2) : __fdiv_rn(num, den2);
+                    acc[v] = fmaf(phi, u.w26[n], acc[v]);
+                }
+                n++;
+            }
+        }
+    }
+}
+
 __global__ void k_rdp(const float *__restrict__ f, float *__restrict__ grad, int nx, int ny,
                       int nz, UpdateArgs u, float scale) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -554,6 +597,8 @@ cudaError_t launch_rdp(const float *f, float *grad, int nx, int ny, int nz, cons
 }
 
 // Update epilogue shared by the gather kernel and the standalone update kernel.
+// PRIOR = false compiles out the RDP term (callers that never see BSREM with a prior).
+template <bool PRIOR = true>
 __device__ __forceinline__ void apply_update(int mode, const UpdateArgs &u, size_t i, int x,
                                              int y, int z, int nx, int ny, int nz, float bp,
                                              float *out) {
@@ -571,7 +616,7 @@ __device__ __forceinline__ void apply_update(int mode, const UpdateArgs &u, size
     } else {  // B2_BSREM
         float f = u.f_in[i], nb = u.nbp[i];
         float grad = __fsub_rn(bp, nb);
-        if (u.prior) {
+        if (PRIOR && u.prior) {
             float v = __fmul_rn(__fmul_rn(u.beta, u.w_m),
                                 rdp_sum(u.f_in, nx, ny, nz, x, y, z, f, u));
             if (u.fov) v = __fmul_rn(v, u.fov[i]);
@@ -584,10 +629,45 @@ __device__ __forceinline__ void apply_update(int mode, const UpdateArgs &u, size
     }
 }
 
+// apply_update for the z quad z..z+3 (z % 4 == 0, nz % 4 == 0).  PRIOR (BSREM with the
+// RDP prior): the prior term comes from rdp_sum4, one neighbourhood load for the four
+// voxels; a separate instantiation, so the other modes keep their register count.
+template <bool PRIOR>
+__device__ __forceinline__ void apply_update4(int mode, const UpdateArgs &u, size_t i, int x,
+                                              int y, int z, int nx, int ny, int nz, float4 bp4,
+                                              float *out) {
+    const float bp[4] = {bp4.x, bp4.y, bp4.z, bp4.w};
+    if constexpr (!PRIOR) {
+#pragma unroll
+        for (int v = 0; v < 4; v++)
+            apply_update<false>(mode, u, i + v, x, y, z + v, nx, ny, nz, bp[v], out);
+        return;
+    }
+    float f[4], rdp[4];
+#pragma unroll
+    for (int v = 0; v < 4; v++) f[v] = u.f_in[i + v];
+    rdp_sum4(u.f_in, nx, ny, nz, x, y, z, f, u, rdp);
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+        float b = bp[v];
+        if (u.acc) b = __fadd_rn(u.acc[i + v], b);
+        const float nb = u.nbp[i + v];
+        float grad = __fsub_rn(b, nb);
+        float pv = __fmul_rn(__fmul_rn(u.beta, u.w_m), rdp[v]);
+        if (u.fov) pv = __fmul_rn(pv, u.fov[i + v]);
+        grad = __fsub_rn(grad, pv);
+        const float pre = __fmul_rn(
+            f[v], __fdiv_rn(u.relax, __fadd_rn(__fmul_rn(u.w_m, u.nbp_sum[i + v]), kDelta)));
+        const float fn = __fadd_rn(f[v], __fmul_rn(pre, grad));
+        u.f_out[i + v] = fn <= u.floor_v ? u.floor_v : fn;
+    }
+}
+
 // ------------------------------------------------------------- B2 gather
 // Reference back-projector: for every object voxel, bilinear sample of W at the
 // back-rotation (angle 270 - beta) of each angle of the group, summed.  Threads own
 // (x, y, z quad); two angles are sampled before accumulating to keep loads in flight.
+template <bool PRIOR>
 __global__ void __launch_bounds__(256)
     k_b2_gather4(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
                  int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
@@ -629,10 +709,7 @@ __global__ void __launch_bounds__(256)
         bp.w = __fadd_rn(bp.w, v1.w);
     }
     const size_t i = ((size_t)x * N + y) * nz + z;
-    apply_update(mode, u, i, x, y, z, N, N, nz, bp.x, out);
-    apply_update(mode, u, i + 1, x, y, z + 1, N, N, nz, bp.y, out);
-    apply_update(mode, u, i + 2, x, y, z + 2, N, N, nz, bp.z, out);
-    apply_update(mode, u, i + 3, x, y, z + 3, N, N, nz, bp.w, out);
+    apply_update4<PRIOR>(mode, u, i, x, y, z, N, N, nz, bp, out);
 }
 
 __global__ void __launch_bounds__(256)
@@ -664,7 +741,10 @@ cudaError_t launch_b2_gather(const SpectDev &g, const float *W, const int *alist
     dim3 block(32, 8);
     if (g.nz % 4 == 0) {
         dim3 grid((g.nz / 4 + 31) / 32, (g.N + 7) / 8, g.N);
-        k_b2_gather4<<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
+        if (mode == B2_BSREM && u.prior)
+            k_b2_gather4<true><<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
+        else
+            k_b2_gather4<false><<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
     } else {
         dim3 grid((g.nz + 31) / 32, (g.N + 7) / 8, g.N);
         k_b2_gather<<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
