@@ -352,22 +352,40 @@ extern "C" int gb_debug_b1_phase_reset(void) {
 
 // -------------------------------------------------------------- B1 (no PSF)
 // W[slot][xp][y][z] = P[y - pad][z] * A (rows [pad, pad+N) are the stored rows).
-__global__ void k_b1_nopsf(SpectDev g, const float *__restrict__ proj,
-                           const int *__restrict__ alist, float *__restrict__ W) {
+// Without PSF: W[xp][y][z] = A (.) P; a thread per (row, z) or, with nz % 4 == 0, per
+// (row, z quad) (16-byte loads and stores).
+template <bool VEC>
+__global__ void __launch_bounds__(256)
+    k_b1_nopsf(SpectDev g, const float *__restrict__ proj, const int *__restrict__ alist,
+               float *__restrict__ W) {
+    constexpr int V = VEC ? 4 : 1;
     const int slot = blockIdx.z, xp = blockIdx.y;
+    const int nzv = g.nz / V;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.nya * g.nz) return;
-    const int r = i / g.nz, z = i % g.nz;
+    if (i >= g.nya * nzv) return;
+    const int r = i / nzv, z = (i % nzv) * V;
     const int y = g.ya_lo + r;
     const int ga = alist[slot];
     if (i == 0) g.wrange[(size_t)slot * g.Lp + xp] = make_int2(0, g.nya);
-    float v = 0.f;
-    if (y >= g.pad && y < g.pad + g.N) {
-        v = proj[((size_t)slot * g.N + (y - g.pad)) * g.nz + z];
-        if (g.att)
-            v = __fmul_rn(v, __ldg(g.A + (((size_t)ga * g.Lp + xp) * g.nya + r) * g.nz + z));
+    float *wp = W + (((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z;
+    const bool in = y >= g.pad && y < g.pad + g.N;
+    const float *pp = proj + ((size_t)slot * g.N + (y - g.pad)) * g.nz + z;
+    const float *ap = g.att ? g.A + (((size_t)ga * g.Lp + xp) * g.nya + r) * g.nz + z : nullptr;
+    if constexpr (VEC) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (in) {
+            v = *reinterpret_cast<const float4 *>(pp);
+            if (g.att) v = mul4(v, __ldg(reinterpret_cast<const float4 *>(ap)));
+        }
+        *reinterpret_cast<float4 *>(wp) = v;
+    } else {
+        float v = 0.f;
+        if (in) {
+            v = *pp;
+            if (g.att) v = __fmul_rn(v, __ldg(ap));
+        }
+        *wp = v;
     }
-    W[(((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z] = v;
 }
 
 template <int K>
@@ -440,8 +458,14 @@ size_t b1_psf_smem_bytes(int K, int N, int Zt) {
 cudaError_t launch_b1(const SpectDev &g, const float *proj, const int *alist, int n_slots,
                       const int4 *items, int n_items, int Zt, float *W, cudaStream_t st) {
     if (!g.psf) {
-        dim3 grid((g.nya * g.nz + 255) / 256, g.Lp, n_slots);
-        k_b1_nopsf<<<grid, 256, 0, st>>>(g, proj, alist, W);
+        // a user projection pointer may not be 16-byte aligned: scalar kernel then
+        if (g.nz % 4 == 0 && ((uintptr_t)proj & 15) == 0) {
+            dim3 grid((g.nya * (g.nz / 4) + 255) / 256, g.Lp, n_slots);
+            k_b1_nopsf<true><<<grid, 256, 0, st>>>(g, proj, alist, W);
+        } else {
+            dim3 grid((g.nya * g.nz + 255) / 256, g.Lp, n_slots);
+            k_b1_nopsf<false><<<grid, 256, 0, st>>>(g, proj, alist, W);
+        }
         return cudaGetLastError();
     }
     switch (g.K) {

@@ -25,32 +25,64 @@ GB_FOR_EACH_K(GB_DECL_FWD)
 #undef GB_DECL_FWD
 
 // ------------------------------------------------------------- without PSF
-// One thread per output (y, z) of an item's planes; A read on the fly.
+// One thread per output (y, z) of an item's planes, or per (y, z quad) with nz % 4 == 0;
+// A read on the fly.  The samples of PU planes are gathered before they are added, in
+// plane order, so those loads are in flight together.
+template <bool VEC>
 __global__ void __launch_bounds__(256)
     k_fwd_nopsf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
                 const int4 *__restrict__ items, float *__restrict__ partials) {
+    constexpr int V = VEC ? 4 : 1, PU = VEC ? 4 : 8;
     const int4 item = items[blockIdx.x];
     const int ga = alist[item.x];
-    const int N = g.N, nz = g.nz;
+    const int N = g.N, nz = g.nz, nzv = nz / V;
     const int i = blockIdx.y * blockDim.x + threadIdx.x;
-    if (i >= N * nz) return;
-    const int y = i / nz, z = i % nz;
+    if (i >= N * nzv) return;
+    const int y = i / nzv, z = (i % nzv) * V;
     float th[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * ga + k];
     const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
     const int yp = g.pad + y;
     const float lc = g.lin[yp];
-    float acc = 0.f;
-    for (int xp = item.y; xp < item.z; ++xp) {
-        float ix, iy;
-        rot_coords(th, g.lin[xp], lc, g.half, ix, iy);
-        Bilin b = bilin(ix, iy);
-        float v = sample(f, N, N, nz, g.pad, g.pad, b, z);
-        if (A) v = __fmul_rn(v, __ldg(A + ((size_t)xp * g.nya + (yp - g.ya_lo)) * nz + z));
-        acc += v;
+    float acc[V];
+#pragma unroll
+    for (int w = 0; w < V; w++) acc[w] = 0.f;
+    for (int x0 = item.y; x0 < item.z; x0 += PU) {
+        float v[PU][V];
+#pragma unroll
+        for (int u = 0; u < PU; u++) {
+            const int xp = min(x0 + u, item.z - 1);
+            float ix, iy;
+            rot_coords(th, g.lin[xp], lc, g.half, ix, iy);
+            const Bilin b = bilin(ix, iy);
+            const size_t ao = ((size_t)xp * g.nya + (yp - g.ya_lo)) * nz + z;
+            if constexpr (VEC) {
+                float4 s4;
+                sample4(f, N, N, nz, g.pad, g.pad, b, z, s4);
+                if (A) s4 = mul4(s4, __ldg(reinterpret_cast<const float4 *>(A + ao)));
+                v[u][0] = s4.x;
+                v[u][1] = s4.y;
+                v[u][2] = s4.z;
+                v[u][3] = s4.w;
+            } else {
+                float s1 = sample(f, N, N, nz, g.pad, g.pad, b, z);
+                if (A) s1 = __fmul_rn(s1, __ldg(A + ao));
+                v[u][0] = s1;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < PU; u++) {
+            if (x0 + u >= item.z) break;
+#pragma unroll
+            for (int w = 0; w < V; w++) acc[w] += v[u][w];
+        }
     }
-    partials[(size_t)blockIdx.x * N * nz + i] = acc;
+    float *out = partials + (size_t)blockIdx.x * N * nz + (size_t)y * nz + z;
+    if constexpr (VEC)
+        *reinterpret_cast<float4 *>(out) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    else
+        out[0] = acc[0];
 }
 
 // --------------------------------------------------------------- reduction
@@ -145,8 +177,13 @@ cudaError_t setup_fwd(int K, size_t smem, int tpb) {
 cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, const int4 *items,
                        int n_items, int Zt, int tpb, float *partials, cudaStream_t st) {
     if (!g.psf) {
-        dim3 grid(n_items, (g.N * g.nz + 255) / 256);
-        k_fwd_nopsf<<<grid, 256, 0, st>>>(g, f, alist, items, partials);
+        if (g.nz % 4 == 0) {
+            dim3 grid(n_items, (g.N * (g.nz / 4) + 255) / 256);
+            k_fwd_nopsf<true><<<grid, 256, 0, st>>>(g, f, alist, items, partials);
+        } else {
+            dim3 grid(n_items, (g.N * g.nz + 255) / 256);
+            k_fwd_nopsf<false><<<grid, 256, 0, st>>>(g, f, alist, items, partials);
+        }
         return cudaGetLastError();
     }
     switch (g.K) {

@@ -184,9 +184,10 @@ static void split_planes(const std::vector<double> &w, int c, int slot,
     }
 }
 
-// Chunks per angle for the plain (no PSF) forward: many 256-thread blocks per SM.
+// Chunks per angle for the plain (no PSF) forward: many 256-thread blocks per SM (a
+// thread per z quad when nz % 4 == 0).
 static int nopsf_chunks(const gb_spect_plan *p, int n_sel) {
-    int gz = (p->N * p->nz + 255) / 256;
+    int gz = (p->N * (p->nz % 4 == 0 ? p->nz / 4 : p->nz) + 255) / 256;
     int c = (8 * p->sm_count + n_sel * gz - 1) / std::max(1, n_sel * gz);
     return std::max(1, std::min(c, std::max(1, p->Lp / 4)));
 }
