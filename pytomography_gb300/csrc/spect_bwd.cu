@@ -662,9 +662,10 @@ __device__ __forceinline__ void apply_update4(int mode, const UpdateArgs &u, siz
                                               float *out) {
     const float bp[4] = {bp4.x, bp4.y, bp4.z, bp4.w};
     if constexpr (!PRIOR) {
-#pragma unroll
-        for (int v = 0; v < 4; v++)
-            apply_update<false>(mode, u, i + v, x, y, z + v, nx, ny, nz, bp[v], out);
+        apply_update(mode, u, i, x, y, z, nx, ny, nz, bp[0], out);
+        apply_update(mode, u, i + 1, x, y, z + 1, nx, ny, nz, bp[1], out);
+        apply_update(mode, u, i + 2, x, y, z + 2, nx, ny, nz, bp[2], out);
+        apply_update(mode, u, i + 3, x, y, z + 3, nx, ny, nz, bp[3], out);
         return;
     }
     float f[4], rdp[4];
@@ -695,8 +696,8 @@ template <bool PRIOR>
 __global__ void __launch_bounds__(256)
     k_b2_gather4(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
                  int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
-    const int q = blockIdx.x * 32 + threadIdx.x;
-    const int y = blockIdx.y * 8 + threadIdx.y;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int x = blockIdx.z;
     const int N = g.N, nz = g.nz;
     if (4 * q >= nz || y >= N) return;
@@ -764,7 +765,13 @@ cudaError_t launch_b2_gather(const SpectDev &g, const float *W, const int *alist
                              float *out, int mode, const UpdateArgs &u, cudaStream_t st) {
     dim3 block(32, 8);
     if (g.nz % 4 == 0) {
-        dim3 grid((g.nz / 4 + 31) / 32, (g.N + 7) / 8, g.N);
+        // blocks of 256 threads shaped to the z quads of a row: when the quads of a row
+        // divide a warp (1, 2, 4, 8 or 16), a warp takes whole rows and no lane idles
+        const int qx = g.nz / 4;
+        const bool packed = qx < 32 && 32 % qx == 0;
+        const dim3 b4(packed ? qx : 32, packed ? 256 / qx : 8);
+        dim3 grid((qx + b4.x - 1) / b4.x, (g.N + b4.y - 1) / b4.y, g.N);
+        block = b4;
         if (mode == B2_BSREM && u.prior)
             k_b2_gather4<true><<<grid, block, 0, st>>>(g, W, alist, n_slots, out, mode, u);
         else
