@@ -121,9 +121,54 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
         i0 = max(i0, ja);
         i1 = min(i1, jb);
     }
+    float acc = 0.f;
+    if constexpr (!BACK) {
+        // Forward: the samples of PU consecutive planes are loaded together, then added
+        // in plane order, corner by corner (the same sums as one plane at a time).
+        constexpr int PU = 4;
+        for (int i = i0; i <= i1; i += PU) {
+            float wv[PU], wq[PU][4], vv[PU][4];
+            bool ok[PU], in[PU][4];
+#pragma unroll
+            for (int u = 0; u < PU; u++) {
+                const int ip = i + u;
+                float w = cf;
+                ok[u] = ip <= i1;
+                if (TOF && ok[u]) {
+                    const float as = fabsf(fmaf((float)ip, ds, s0));
+                    if (as > lim) {
+                        ok[u] = false;
+                    } else {
+                        const float t = as * g.tof_inv_step;
+                        const int m = min((int)t, kTofTab);
+                        const float t0w = __ldg(g.tof_tab + m), t1w = __ldg(g.tof_tab + m + 1);
+                        w *= fmaf(t - (float)m, t1w - t0w, t0w);
+                    }
+                }
+                wv[u] = w;
+                const float fa = fmaf((float)ip, dfa, fa0), fb = fmaf((float)ip, dfb, fb0);
+                const float ga = floorf(fa), gb2 = floorf(fb);
+                const int ia = (int)ga, ib = (int)gb2;
+                const float wa = fa - ga, wb = fb - gb2;
+                const int base = ip * sk;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int ja = ia + (q & 1), jb = ib + (q >> 1);
+                    in[u][q] = ok[u] && (unsigned)ja < (unsigned)na && (unsigned)jb < (unsigned)nb;
+                    wq[u][q] = ((q & 1) ? wa : 1.f - wa) * ((q >> 1) ? wb : 1.f - wb);
+                    vv[u][q] = in[u][q] ? __ldg(cimg + base + ja * sa + jb * sb) : 0.f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < PU; u++)
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (in[u][q]) acc += wv[u] * wq[u][q] * vv[u][q];
+        }
+        return acc;
+    }
     // the bilinear pair axis that is z (stride 1), if any: corners along it are neighbours
     const bool zb = sb == 1, za = sa == 1;
-    float acc = 0.f;
     for (int i = i0; i <= i1; i++) {
         float w = cf;
         if (TOF) {
