@@ -37,78 +37,12 @@ __device__ __forceinline__ void tier_dispatch(int tier, F &&f) {
     }
 }
 
+// Scalar passes for CTAs whose register budget holds no tap registers (768-thread forward);
+// the taps are read from shared memory (a broadcast load) inside the tap loop.
+//
 // First pass: blur along the S row axis for output row blocks [b_lo, b_hi) and columns
 // [c_lo, c_hi); writes Tt[c][block * OB + j] (transposed).  Warp-tasks are (32-column
 // chunk, row block), lanes take consecutive columns.
-template <int K, int KK, int OB>
-__device__ __forceinline__ void blur_first(const float *__restrict__ S, float *__restrict__ Tt,
-                                           const float *__restrict__ tap, int SC, int TS,
-                                           int c_lo, int c_hi, int b_lo, int b_hi, int warp,
-                                           int lane, int nwarp) {
-    constexpr int OFF = (K - KK) / 2;
-    float w[KK];
-#pragma unroll
-    for (int t = 0; t < KK; t++) w[t] = tap[OFF + t];
-    const int nb = b_hi - b_lo;
-    const int ncc = (c_hi - c_lo + 31) >> 5;
-    for (int p = warp; p < ncc * nb; p += nwarp) {
-        const int cc = p % ncc, yb = b_lo + p / ncc;
-        const int c = c_lo + (cc << 5) + lane;
-        if (c >= c_hi) continue;
-        const float *sp = S + (yb * OB + OFF) * SC + c;
-        float win[OB + KK - 1];
-#pragma unroll
-        for (int i = 0; i < OB + KK - 1; i++) win[i] = sp[i * SC];
-        float o[OB];
-#pragma unroll
-        for (int j = 0; j < OB; j++) o[j] = 0.f;
-#pragma unroll
-        for (int t = 0; t < KK; t++)
-#pragma unroll
-            for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
-        float *tq = Tt + c * TS + yb * OB;
-#pragma unroll
-        for (int j = 0; j < OB; j++) tq[j] = o[j];
-    }
-}
-
-// Second pass of one task: blur along the Tt row axis for OB consecutive outputs
-// starting at Tt row `row0` (taps of the full bucket start there), column `col`.
-template <int K, int KK, int OB>
-__device__ __forceinline__ void blur_second(const float *__restrict__ Tt,
-                                            const float (&w)[KK], int TS, int row0, int col,
-                                            float (&o)[OB]) {
-    constexpr int OFF = (K - KK) / 2;
-    const float *tq = Tt + (row0 + OFF) * TS + col;
-    float win[OB + KK - 1];
-#pragma unroll
-    for (int i = 0; i < OB + KK - 1; i++) win[i] = tq[i * TS];
-#pragma unroll
-    for (int j = 0; j < OB; j++) o[j] = 0.f;
-#pragma unroll
-    for (int t = 0; t < KK; t++)
-#pragma unroll
-        for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
-}
-
-// Same as blur_second, accumulating into o (o += blur) instead of overwriting it.
-template <int K, int KK, int OB>
-__device__ __forceinline__ void blur_second_acc(const float *__restrict__ Tt,
-                                                const float (&w)[KK], int TS, int row0, int col,
-                                                float (&o)[OB]) {
-    constexpr int OFF = (K - KK) / 2;
-    const float *tq = Tt + (row0 + OFF) * TS + col;
-    float win[OB + KK - 1];
-#pragma unroll
-    for (int i = 0; i < OB + KK - 1; i++) win[i] = tq[i * TS];
-#pragma unroll
-    for (int t = 0; t < KK; t++)
-#pragma unroll
-        for (int j = 0; j < OB; j++) o[j] = fmaf(w[t], win[j + t], o[j]);
-}
-
-// Variants for CTAs whose register budget holds no tap registers (768-thread forward):
-// the taps are read from shared memory (a broadcast load) inside the tap loop.
 template <int K, int KK, int OB>
 __device__ __forceinline__ void blur_first_st(const float *__restrict__ S, float *__restrict__ Tt,
                                               const float *__restrict__ tap, int SC, int TS,
@@ -140,7 +74,9 @@ __device__ __forceinline__ void blur_first_st(const float *__restrict__ S, float
     }
 }
 
-// blur_second with shared-memory taps; ACC: o += blur instead of o = blur
+// Second pass of one task: blur along the Tt row axis for OB consecutive outputs starting
+// at Tt row `row0` (taps of the full bucket start there), column `col`; ACC: o += blur
+// instead of o = blur.
 template <int K, int KK, int OB, bool ACC>
 __device__ __forceinline__ void blur_second_st(const float *__restrict__ Tt,
                                                const float *__restrict__ wsm, int TS, int row0,
