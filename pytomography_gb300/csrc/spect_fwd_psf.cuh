@@ -70,8 +70,10 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 //                z quads; SC a multiple of 32: 128-byte aligned rows).  Before phase 1 of
 //                a plane, the attenuation rows of that plane are copied into S by 2-D TMA
 //                boxes of kBoxRows full S rows (`tmA`: A viewed as [n_angles*Lp*nya][nz],
-//                z outside [0, nz) reads as zero) and multiplied in place.
+//                z outside [0, nz) reads as zero; one 1-D bulk copy per row instead when a
+//                row is wider than a box, SC > 256) and multiplied in place.
 //   Tt [TR][TS]: y-blurred plane, transposed; row c <-> z = z0 - HP + c, column = output y
+//                (TS even with 512 threads: float2 row pairs)
 //   taps [2][2][K]: double-buffered y / z taps of the current plane
 //   one mbarrier for the TMA copies
 // Per plane only the rows the rotated object square can reach are sampled / blurred.
