@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "OSEM subiter/s at 128^3x120 ang (att+PSF)"
 # DRAM bytes (read + write) of one 12-angle k_fwd_psf launch from the ncu capture summarised
 # in profiles/spect_osem_128cube_120ang.md
-FWD_DRAM_BYTES_PER_LAUNCH = 114.885e6 + 3.163e6
+FWD_DRAM_BYTES_PER_LAUNCH = 114.981e6 + 3.262e6
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
