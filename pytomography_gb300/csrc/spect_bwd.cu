@@ -231,12 +231,14 @@ __global__ void __launch_bounds__(512, 1)
         }
         int tier = kTiers - 1;
         if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : kTiers - 1;
-        // column pairs, blocks of OP = OB / 2 rows (as many warp-tasks as scalar blocks of OB)
+        // y blur over column pairs in blocks of OB rows (8-row blocks measured faster than 4:
+        // fewer shared-memory loads per output outweigh the coarser task balance); the z blur
+        // below uses blocks of OP = OB / 2 z values
         constexpr int OP = OB / 2;
         tier_dispatch<K>(tier, [&](auto kk) {
             constexpr int KK = decltype(kk)::value;
-            blur_first2<K, KK, OP>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo * 2, b_hi * 2, warp,
-                                   lane, nwarp);
+            blur_first2<K, KK, OB>(S, Tt, tap, SC, TS, cz_lo, cz_hi, b_lo, b_hi, warp, lane,
+                                   nwarp);
         });
         GB_B1T(8, rb - ra + 1);
         GB_B1T(9, (rb - ra + 1) * tier_taps(K, tier));
