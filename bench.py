@@ -386,7 +386,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gbtomo", choices=["gbtomo", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--out", default=os.path.join(ROOT, "bench_out"),
+                    help="folder for the clock samples of the timed region (clocks.csv)")
     ap.add_argument("--profile-case", action="store_true",
                     help="run 3 fused sub-iterations of the workload and exit (for ncu)")
     ap.add_argument("--workload", default="osem128",  # osem64: the 64^3 / 64-angle att case
