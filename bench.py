@@ -36,8 +36,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "OSEM subiter/s at 128^3x120 ang (att+PSF)"
-# DRAM bytes (read + write) of one 12-angle k_fwd_psf launch from the ncu capture summarised
-# in profiles/spect_osem_128cube_120ang.md
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 12-angle k_fwd_psf launch
+# of this workload, from a separate ncu capture of the same kernel (a constant: this
+# script does not run ncu)
 FWD_DRAM_BYTES_PER_LAUNCH = 114.981e6 + 3.262e6
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
@@ -72,48 +73,118 @@ def alg_bytes_subiter(n=128, n_sel=12, att=1):
 
 
 class Clocks:
-    """nvidia-smi sampler running during the timed region."""
+    """SM clock and clock-event reasons of this process's GPU, sampled about every
+    millisecond while the timed region runs (NVML through ctypes, read-only queries;
+    nvidia-smi at 100 ms as a fallback).  The device is addressed by its UUID, so the
+    sampler reads the leased GPU even when CUDA_VISIBLE_DEVICES renumbers it."""
 
-    def __init__(self, path):
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, path, device):
+        import torch
         self.path = path
-        self.proc = None
+        self.samples = []  # (sm MHz, reason bits)
+        self.max_mhz = None
+        self.source = None
+        try:
+            self.uuid = "GPU-" + str(torch.cuda.get_device_properties(device).uuid)
+        except Exception:
+            self.uuid = None
+        self._nvml = None
+        self._thread = None
+        self._proc = None
+
+    def _nvml_open(self):
+        import ctypes
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0 or not self.uuid:
+            return None
+        h = ctypes.c_void_p()
+        if nv.nvmlDeviceGetHandleByUUID(self.uuid.encode(), ctypes.byref(h)) != 0:
+            return None
+        mx = ctypes.c_uint(0)
+        if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:  # 1 = SM clock
+            self.max_mhz = float(mx.value)
+        fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        return nv, h, fn
 
     def __enter__(self):
+        import ctypes
+        import threading
+        try:
+            self._nvml = self._nvml_open()
+        except Exception:
+            self._nvml = None
+        if self._nvml is not None:
+            nv, h, reasons_fn = self._nvml
+            self.source = "nvml, ~1 ms"
+            self._stop = threading.Event()
+
+            def loop():
+                mhz, bits = ctypes.c_uint(0), ctypes.c_ulonglong(0)
+                while not self._stop.is_set():
+                    if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0 and \
+                            reasons_fn(h, ctypes.byref(bits)) == 0:
+                        self.samples.append((float(mhz.value), int(bits.value)))
+                    time.sleep(0.001)
+
+            self._thread = threading.Thread(target=loop, daemon=True)
+            self._thread.start()
+            time.sleep(0.005)
+            return self
         try:
             self.fh = open(self.path, "w")
-            self.proc = subprocess.Popen(
+            self._proc = subprocess.Popen(
                 ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
                  "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "100", "-i", "0"],
+                 "--format=csv,noheader,nounits", "-lms", "100", "-i", self.uuid or "0"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
+            self.source = "nvidia-smi, 100 ms"
         except Exception:
-            self.proc = None
+            self._proc = None
         time.sleep(0.3)
         return self
 
     def __exit__(self, *a):
-        if self.proc is not None:
-            self.proc.terminate()
-            self.proc.wait()
+        if self._thread is not None:
+            self._stop.set()
+            self._thread.join()
+        if self._proc is not None:
+            self._proc.terminate()
+            self._proc.wait()
             self.fh.close()
+            try:
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                         "sw_power_cap"]
+                bits = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+                        "hw_thermal_slowdown": 0x40}
+                for r in open(self.path).read().strip().splitlines():
+                    f = r.split(",")
+                    self.max_mhz = float(f[2])
+                    b = 0
+                    for k, name in enumerate(names):
+                        if f[5 + k].strip() == "Active":
+                            b |= bits[name]
+                    self.samples.append((float(f[1]), b))
+            except Exception:
+                pass
 
     def summary(self):
-        try:
-            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
-            sm = [float(r[1]) for r in rows]
-            mx = float(rows[0][2])
-            reasons = set()
-            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-            for r in rows:
-                for k, name in enumerate(names):
-                    if r[5 + k].strip() == "Active":
-                        reasons.add(name)
-            return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                    "samples": len(rows)}
-        except Exception as e:  # no nvidia-smi
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(e)[:80]}
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [],
+                    "samples": 0, "source": self.source}
+        reasons = set()
+        for _, b in self.samples:
+            for bit, name in self.REASONS.items():
+                if b & bit:
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median([m for m, _ in self.samples])),
+                "sm_max_mhz": self.max_mhz, "reasons": sorted(reasons),
+                "samples": len(self.samples), "source": self.source, "device": self.uuid}
 
 
 class CpuSubiter:
@@ -500,7 +571,7 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    clocks = Clocks(os.path.join(args.out, "clocks.csv")) if rank == 0 else None
+    clocks = Clocks(os.path.join(args.out, "clocks.csv"), dev) if rank == 0 else None
     os.makedirs(args.out, exist_ok=True)
     if clocks:
         clocks.__enter__()
@@ -619,7 +690,9 @@ def main():
                          "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                          "peak_kind": peak_kind,
                          "traffic": FWD_DRAM_BYTES_PER_LAUNCH if w.shape[0] == 128 else None,
-                         "traffic_source": "ncu dram__bytes_read+write, one launch",
+                         "traffic_source": "constant from a separate ncu capture of one "
+                                           "launch (dram__bytes_read.sum + "
+                                           "dram__bytes_write.sum); not measured by this run",
                          "alg_bytes_per_launch": fwd_bytes, "launch_ms": fwd_ms},
             "backward_ms": bwd_ms,
             "alg_gbs_per_subiter": sub_bytes / (fused_ms / 1000) / 1e9,

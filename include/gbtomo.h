@@ -37,6 +37,15 @@ const char *gb_last_error(void);
 /* Library version string. */
 const char *gb_version(void);
 
+/* Host-side fault injection for tests of the error paths (no counterpart in the reference,
+ * which has no native code).  Arms `site` ("alloc": a device allocation at plan creation,
+ * subset setup or tuning returns GB_ERR_OOM; "launch": a projector / update entry point
+ * returns GB_ERR_CUDA before launching anything; "arg": such an entry point returns
+ * GB_ERR_ARG) so that its nth check from now on fails, once; nth = 0 disarms it.  The
+ * environment variable GBTOMO_INJECT ("alloc:1,launch:2") arms sites the same way when the
+ * library first checks one.  Nothing here touches the GPU. */
+gb_status gb_inject_fault(const char *site, int32_t nth);
+
 /* ------------------------------------------------------------------ SPECT */
 
 typedef struct gb_spect_plan gb_spect_plan;
@@ -83,6 +92,14 @@ gb_status gb_spect_plan_destroy(gb_spect_plan *plan);
  * bounded wait on its TMA copies gave up (the kernel then returned without output).
  * No counterpart in the reference (which has no device code). */
 gb_status gb_spect_device_status(gb_spect_plan *plan, int32_t *code);
+/* Reset the device error word to 0. */
+gb_status gb_spect_clear_device_status(gb_spect_plan *plan);
+/* Test hook of the bounded waits (no counterpart in the reference): skip_first_copy = 1
+ * makes the fused forward projector (attenuation before PSF, nz % 4 == 0) leave its first
+ * attenuation copy of every work item unissued, so its wait for that copy runs out after
+ * wait_polls polls (each at most 20 us; 0 restores the default of 65536) and the kernel
+ * returns with the error word set to 1.  Nothing is left in flight. */
+gb_status gb_spect_set_debug(gb_spect_plan *plan, int32_t skip_first_copy, int32_t wait_polls);
 
 /* Interleaved angle subsets indices[i::n_subsets]
  * (spect_system_matrix.py:58-71).  n_subsets >= 1. */
@@ -124,8 +141,8 @@ gb_status gb_spect_forward(gb_spect_plan *plan, const float *object, float *proj
                            int32_t subset, gb_stream_t stream);
 
 /* Same projection as gb_spect_forward, for callers that must not allocate device memory
- * while they run (graph-captured or pool-restricted code, processes whose memory belongs
- * to another allocator).  No counterpart in the reference.  Its partial sums use a fixed
+ * while they run (code on a pool-restricted stream, processes whose device memory belongs
+ * to another allocator, services that budget every allocation up front).  No counterpart in the reference.  Its partial sums use a fixed
  * 16 MiB device array compiled into the library instead of the plan's scratch; calls
  * needing more than 4,194,304 floats of partials (the plan's work items for the subset,
  * at least one per angle, times nx * nz) return GB_ERR_SHAPE.  Calls share that array: overlapping calls on the GPU race.  The first
@@ -154,6 +171,34 @@ gb_status gb_spect_backward(gb_spect_plan *plan, const float *proj, float *objec
 gb_status gb_spect_osem_step(gb_spect_plan *plan, float *object, const float *projections,
                              const float *additive, const float *norm_bp, int32_t subset,
                              float *predicted, gb_stream_t stream);
+
+/* ------------------------------------------------- per-angle obj2obj plugins
+ * The two plugins of the reference's per-angle loop
+ * (projectors/SPECT/spect_system_matrix.py:145-154 and 188-198), applied to an object
+ * that the caller has already padded and rotated into the detector frame of one angle:
+ * [L][ny][nz] device arrays, x (the first axis) towards the detector.  They need no plan.
+ *
+ * Attenuation, SPECTAttenuationTransform.forward / backward
+ * (transforms/SPECT/attenuation.py:72-115 with get_prob_of_detection_matrix, :11-21, and
+ * rev_cumsum, utils/misc.py:8-19):
+ *   out[x][y][z] = in[x][y][z] * exp(-(sum_{k>=x} t_k - t_x / 2)),  t_k = mu_rot[k][y][z] * dx,
+ * where mu_rot is mu ([n][n][nz], device, cm^-1) zero-padded by `pad` in x and y
+ * (L = n + 2 pad) and sampled at the kornia-convention rotation `theta` (host [6], the
+ * forward-projector matrix of the angle, as gb_spect_desc.theta_fwd) over the grid `lin`
+ * (device [L], linspace(-1, 1, L)).  The factor is recomputed from mu on every call.
+ * Backward is the same diagonal operator.  in may equal out. */
+gb_status gb_spect_attenuation_apply(const float *mu, int32_t n, int32_t nz, int32_t pad,
+                                     float dx, const float *theta, const float *lin,
+                                     const float *in, float *out, gb_stream_t stream);
+/* Depth-dependent separable PSF, SPECTPSFTransform.forward / backward
+ * (transforms/SPECT/psf.py:199-231 -> Seperable1DBlurNet.forward, :27-41): per plane x,
+ * a 'same' zero-padded correlation along y with taps_y[x] ([nplanes][ky], device), then
+ * along z with taps_z[x] ([nplanes][kz], device; NULL = the '1D' model, no z blur).
+ * Backward is the same (symmetric taps).  Odd tap counts up to 63; in and out must
+ * differ. */
+gb_status gb_spect_psf_apply(const float *in, float *out, int32_t nplanes, int32_t ny,
+                             int32_t nz, const float *taps_y, int32_t ky, const float *taps_z,
+                             int32_t kz, gb_stream_t stream);
 
 /* Relative-difference prior with Euclidean neighbour weights
  * (priors/nearest_neighbour.py:156-183, 207-220). */

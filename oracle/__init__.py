@@ -45,6 +45,10 @@ def _lib(precision: str) -> ctypes.CDLL:
                                         _real(precision), ctypes.c_double, ctypes.c_char_p,
                                         P, ctypes.c_int, P, ctypes.c_int]
         lib.orc_spect_angle.restype = ctypes.c_int
+        lib.orc_spect_plugin.argtypes = [ctypes.c_int, P, P, P, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, _real(precision), ctypes.c_double, P,
+                                         ctypes.c_int, P, ctypes.c_int]
+        lib.orc_spect_plugin.restype = ctypes.c_int
         R = _real(precision)
         lib.orc_pet_lm.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_int64, P, P, P, P,
                                    P, ctypes.c_int, R, R, R, R, ctypes.c_int]
@@ -171,6 +175,41 @@ class SpectOracle:
     def adjoint(self, g, angle_idx=None):
         """Exact transpose of :meth:`forward`."""
         return self._back(2, g, angle_idx)
+
+
+def spect_plugin(which: str, x, dr, beta_deg, mu=None, pad=None, psf=None, radius=0.0,
+                 psf_2d=True, precision="f64"):
+    """One plugin call on an object already in the detector frame of angle ``beta_deg``
+    (orc_spect_plugin): ``which`` = "att" (SPECTAttenuationTransform.forward,
+    attenuation.py:72-92) or "psf" (SPECTPSFTransform.forward, psf.py:199-214).
+    x: [H, H, Lz] with H = N + 2 pad; pad defaults to the padded frame's."""
+    dt = _np_dtype(precision)
+    lib = _lib(precision)
+    x = np.ascontiguousarray(x, dtype=dt)
+    H, _, nz = x.shape
+    if which == "att":
+        mu = np.ascontiguousarray(mu, dtype=dt)
+        n = mu.shape[0]
+        pad = pad_size(n) if pad is None else int(pad)
+        if n + 2 * pad != H:
+            raise ValueError("object frame does not match mu and pad")
+        wr = wz = None
+        kr = kz = 1
+    else:
+        n, pad = H, 0
+        a, b = psf
+        wr, wz = psf_tables(H, dr[0], dr[2], radius, a, b, two_d=psf_2d)
+        wr = np.ascontiguousarray(wr, dt)
+        wz = None if wz is None else np.ascontiguousarray(wz, dt)
+        kr, kz = wr.shape[1], 1 if wz is None else wz.shape[1]
+    out = np.empty_like(x)
+    rc = lib.orc_spect_plugin(0 if which == "att" else 1, _ptr(x), _ptr(out),
+                              None if mu is None else _ptr(mu), n, nz, pad, dt(dr[0]),
+                              float(beta_deg), None if wr is None else _ptr(wr), kr,
+                              None if wz is None else _ptr(wz), kz)
+    if rc != 0:
+        raise RuntimeError(f"oracle error {rc}")
+    return out
 
 
 def subsets(n_items: int, n_subsets: int):

@@ -247,6 +247,38 @@ int orc_spect_angle(int mode, const REAL *in, REAL *out, const REAL *mu, int N, 
     return 0;
 }
 
+/* The per-angle obj2obj plugins on an object already in the detector frame of one
+ * angle, [H][H][Lz] with H = N + 2 pad (pad = 0: the unpadded frame of
+ * assume_padded=False):
+ *   which 0: attenuation, out = in * exp(-rev_cumsum(mu_rot * dx)), mu [N][N][Lz] zero-padded
+ *            by pad and rotated by beta - 270 (attenuation.py:72-115);
+ *   which 1: the separable PSF with taps wr [H][Kr] and wz [H][Kz] (wz NULL: '1D')
+ *            (psf.py:199-231). */
+int orc_spect_plugin(int which, const REAL *in, REAL *out, const REAL *mu, int N, int Lz,
+                     int pad, REAL dx, double beta_deg, const REAL *wr, int Kr, const REAL *wz,
+                     int Kz) {
+    int H = N + 2 * pad;
+    size_t P = (size_t)H * H * Lz;
+    memcpy(out, in, P * sizeof(REAL));
+    if (which == 1) {
+        psf_blur(out, H, Lz, wr, Kr, wz, Kz);
+        return 0;
+    }
+    if (!mu) return -2;
+    REAL *T = (REAL *)calloc(P, sizeof(REAL));
+    REAL *V = (REAL *)calloc(P, sizeof(REAL));
+    if (!T || !V) return -1;
+    for (int x = 0; x < N; x++)
+        for (int y = 0; y < N; y++)
+            memcpy(T + IDX3(x + pad, y + pad, 0, H, Lz), mu + IDX3(x, y, 0, N, Lz),
+                   sizeof(REAL) * Lz);
+    rotate_stack(T, V, H, Lz, beta_deg - 270.0);
+    atten_factor(V, T, H, Lz, dx);
+    for (size_t i = 0; i < P; i++) out[i] *= T[i];
+    free(T); free(V);
+    return 0;
+}
+
 /* ------------------------------------------------------------------- PET */
 
 /* Joseph ray tracing of one LOR p0 -> p1 through an image with voxel centres at

@@ -81,6 +81,9 @@ SIGNATURES = [
     ("gb_spect_plan_destroy", c_int, [c_void_p]),
     ("gb_spect_set_subsets", c_int, [c_void_p, c_int]),
     ("gb_spect_device_status", c_int, [c_void_p, ctypes.POINTER(c_int)]),
+    ("gb_spect_clear_device_status", c_int, [c_void_p]),
+    ("gb_spect_set_debug", c_int, [c_void_p, c_int, c_int]),
+    ("gb_inject_fault", c_int, [c_char_p, c_int]),
     ("gb_spect_subset_size", c_int, [c_void_p, c_int]),
     ("gb_spect_set_subset_lists", c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     ("gb_starguide_window", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p,
@@ -97,6 +100,10 @@ SIGNATURES = [
     ("gb_spect_bsrem_step", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_float, c_float, ctypes.POINTER(RdpDesc),
                                     c_float, c_int, c_void_p]),
+    ("gb_spect_attenuation_apply", c_int, [c_void_p, c_int, c_int, c_int, c_float, c_void_p,
+                                           c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("gb_spect_psf_apply", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int,
+                                   c_void_p, c_int, c_void_p]),
     ("gb_rdp_gradient", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_float,
                                 c_float, ctypes.POINTER(RdpDesc), c_float, c_void_p]),
     ("gb_rdp_hessian_vector", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_float,

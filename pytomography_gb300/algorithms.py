@@ -73,71 +73,41 @@ class PreconditionedGradientAscentAlgorithm:
     def compute_uncertainty(self, mask: torch.Tensor, data_storage_callback,
                             subiteration_number: int | None = None, return_pct: bool = False,
                             include_additive_term: bool = False, post_recon_filter=None):
-        """Uncertainty of the sum of counts in ``mask`` from the iterates stored by a
-        ``DataStorageCallback`` (preconditioned_gradient_ascent.py:170-215): the
-        variance propagates back through every sub-iteration with the operators Q and B,
-        whose projector calls run on the GPU kernels."""
+        """Standard deviation of the counts m^T f_N in ``mask`` after sub-iteration N,
+        from the iterates and predictions a ``DataStorageCallback`` stored (the method of
+        preconditioned_gradient_ascent.py:170-215).
+
+        Every sub-iteration is a map f_{n+1} = U_n(f_n, g).  The counts' sensitivity to
+        the data is propagated backwards through the chain with the adjoint Jacobians of
+        each stored step (``_StepJacobian``): a running object-space vector q starts at
+        m (or the filtered mask), every step adds its data-space image J_g^T q to the
+        projection-space sensitivity v, and q moves one step back as J_f^T q.  With
+        Poisson data Var(m^T f_N) = sum_i g_i v_i^2 (plus the additive term's variance
+        when requested).  Every operator application is projector calls on the GPU."""
         cb = data_storage_callback
-        if subiteration_number is None:
-            subiteration_number = len(cb.objects) - 1
-        final_recon = cb.objects[subiteration_number].to(_p.device)
+        last = len(cb.objects) - 1 if subiteration_number is None else subiteration_number
+        f_last = cb.objects[last].to(_p.device)
+        q = mask.clone() if post_recon_filter is None else post_recon_filter(mask)
         if post_recon_filter is not None:
-            Q = post_recon_filter(mask)
-            final_recon = post_recon_filter(final_recon)
-        else:
-            Q = mask.clone()
-        V = 0
-        for n in range(subiteration_number, 0, -1):
-            V = V + self._compute_B(Q, cb, n - 1, include_additive_term=include_additive_term)
-            if n > 1:
-                Q = self._compute_Q(Q, cb, n - 1)
-        abs2 = torch.sum(V[0] * self.likelihood.projections * V[0])
+            f_last = post_recon_filter(f_last)
+        v = None
+        for n in reversed(range(last)):  # steps n -> n + 1, newest first
+            step = _StepJacobian(self, cb, n)
+            term = step.data_sensitivity(q, include_additive_term)
+            v = term if v is None else v + term
+            if n > 0:
+                q = step.object_sensitivity(q)
+        variance = torch.sum(v[0] * self.likelihood.projections * v[0])
         if include_additive_term:
-            abs2 = abs2 + torch.sum(self.likelihood.additive_term_variance_estimate(V[1]))
-        unc_abs = torch.sqrt(abs2).item()
+            variance = variance + torch.sum(self.likelihood.additive_term_variance_estimate(v[1]))
+        sd = torch.sqrt(variance).item()
         if not return_pct:
-            return unc_abs
-        return unc_abs, unc_abs / (final_recon * mask).sum().item() * 100
+            return sd
+        return sd, sd / (f_last * mask).sum().item() * 100
 
     def _uncertainty_subset(self, n: int):
+        """Subset index sub-iteration n used (None without subsets)."""
         return None if self.n_subsets == 1 else n % self.n_subsets
-
-    def _compute_Q(self, input, cb, n: int):
-        """Q of the uncertainty recursion (preconditioned_gradient_ascent.py:217-251)."""
-        subset_idx = self._uncertainty_subset(n)
-        f_n = cb.objects[n].to(_p.device)
-        f_next = cb.objects[n + 1].to(_p.device)
-        fp_n = cb.projections_predicted[n].to(_p.device)
-        grad_ff = self.likelihood.compute_gradient_ff(f_n, fp_n, subset_idx)
-        out = input * f_n * self._linear_preconditioner_factor(None, subset_idx)
-        if self.prior is not None:
-            self.prior.set_beta_scale(self.likelihood.system_matrix.get_weighting_subset(subset_idx))
-            self.prior.set_object(f_n)
-            out = grad_ff(out) - self.prior(derivative_order=2)(out)
-        else:
-            out = grad_ff(out)
-        return out + (f_next / (f_n + _p.delta)) * input
-
-    def _compute_B(self, input, cb, n: int, include_additive_term: bool = False):
-        """B of the uncertainty recursion (preconditioned_gradient_ascent.py:253-299)."""
-        sm = self.likelihood.system_matrix
-        subset_idx = self._uncertainty_subset(n)
-        if subset_idx is None:
-            rows = torch.arange(sm.proj_meta.shape[0]).to(torch.long).to(_p.device)
-        else:
-            rows = sm.subset_indices_array[subset_idx]
-        f_n = cb.objects[n].to(_p.device)
-        fp_n = cb.projections_predicted[n].to(_p.device)
-        out = input * f_n * self._linear_preconditioner_factor(None, subset_idx)
-        primary = self.likelihood.compute_gradient_gf(f_n, fp_n, subset_idx)(out)
-        n_out = 2 if include_additive_term else 1
-        total = torch.zeros((n_out, *fp_n.shape[:-3], *sm.proj_meta.shape[-3:]),
-                            device=primary.device)
-        total[0, ..., rows, :, :] = primary
-        if include_additive_term:
-            total[1, ..., rows, :, :] = self.likelihood.compute_gradient_sf(f_n, fp_n,
-                                                                            subset_idx)(out)
-        return total
 
     def _fused_begin(self) -> None:
         pass
@@ -179,6 +149,56 @@ class PreconditionedGradientAscentAlgorithm:
         if self.callback is not None:
             self.callback.finalize(self.object_prediction)
         return self.object_prediction
+
+
+class _StepJacobian:
+    """Adjoint Jacobians of one stored sub-iteration of a linearly preconditioned update
+    f_{n+1} = f_n + f_n c_n (grad L_n(f_n) - grad V(f_n)), clamped, where c_n is the
+    algorithm's preconditioner factor for the step's subset.
+
+    With D = diag(f_n c_n) and the likelihood's curvature blocks at the stored prediction
+    (``PoissonCurvature``):
+      object_sensitivity(q) = (L_ff - V_ff) D q + (f_{n+1} / (f_n + delta)) q
+      data_sensitivity(q)   = [L_gf D q (, L_sf D q)] placed on the subset's projection
+                              rows of full-size projection arrays.
+    The ratio f_{n+1}/f_n stands for the derivative of the update's multiplicative part
+    and, for clamped voxels, for the zero derivative of the clamp."""
+
+    def __init__(self, alg, cb, n: int) -> None:
+        self.alg = alg
+        self.subset_idx = alg._uncertainty_subset(n)
+        self.f = cb.objects[n].to(_p.device)
+        self.f_next = cb.objects[n + 1].to(_p.device) if n + 1 < len(cb.objects) else None
+        self.curv = alg.likelihood._curvature(self.f, cb.projections_predicted[n].to(_p.device),
+                                              self.subset_idx)
+        self.scale = self.f * alg._linear_preconditioner_factor(None, self.subset_idx)
+
+    def object_sensitivity(self, q: torch.Tensor) -> torch.Tensor:
+        dq = q * self.scale
+        out = self.curv.ff(dq)
+        prior = self.alg.prior
+        if prior is not None:
+            sm = self.alg.likelihood.system_matrix
+            prior.set_beta_scale(sm.get_weighting_subset(self.subset_idx))
+            prior.set_object(self.f)
+            out = out - prior(derivative_order=2)(dq)
+        return out + (self.f_next / (self.f + _p.delta)) * q
+
+    def data_sensitivity(self, q: torch.Tensor, include_additive_term: bool) -> torch.Tensor:
+        sm = self.alg.likelihood.system_matrix
+        dq = q * self.scale
+        parts = [self.curv.gf(dq)]
+        if include_additive_term:
+            parts.append(self.curv.sf(dq))
+        full = tuple(sm.proj_meta.shape[-3:])
+        out = torch.zeros((len(parts), *parts[0].shape[:-3], *full), device=parts[0].device)
+        if self.subset_idx is None:
+            rows = torch.arange(full[0], device=out.device)
+        else:
+            rows = sm.subset_indices_array[self.subset_idx].to(out.device)
+        for k, p in enumerate(parts):
+            out[k].index_copy_(out[k].dim() - 3, rows, p)
+        return out
 
 
 class LinearPreconditionedGradientAscentAlgorithm(PreconditionedGradientAscentAlgorithm):
@@ -327,25 +347,29 @@ class PGAAMultiBedSPECT(PreconditionedGradientAscentAlgorithm):
         self._finalize_callback()
         return self.object_prediction
 
+    def _callback_pairs(self):
+        """(bed algorithm, callback) pairs for a list of per-bed callbacks, or
+        [(None, callback)] for one callback that sees the stitched object."""
+        cbs = self.callback
+        if cbs is None:
+            return []
+        if isinstance(cbs, list):
+            return list(zip(self.reconstruction_algorithms, cbs))
+        return [(None, cbs)]
+
     def _multibed_callback(self, n_iter: int, n_subset: int) -> None:
-        if self.callback is None:
-            return
-        if isinstance(self.callback, list):
-            for a, cb in zip(self.reconstruction_algorithms, self.callback):
-                a.callback = cb
-                a._compute_callback(n_iter=n_iter, n_subset=n_subset)
-        else:
-            self.object_prediction = self.callback.run(self.object_prediction, n_iter, n_subset)
+        for alg, cb in self._callback_pairs():
+            if alg is None:  # the stitched reconstruction
+                self.object_prediction = cb.run(self.object_prediction, n_iter, n_subset)
+            else:  # each bed's own iterate
+                alg.callback = cb
+                alg._compute_callback(n_iter=n_iter, n_subset=n_subset)
 
     def _finalize_callback(self) -> None:
-        if self.callback is None:
-            return
-        if isinstance(self.callback, list):
-            for a, cb in zip(self.reconstruction_algorithms, self.callback):
-                a.callback = cb
-                cb.finalize(a.object_prediction)
-        else:
-            self.callback.finalize(self.object_prediction)
+        for alg, cb in self._callback_pairs():
+            if alg is not None:
+                alg.callback = cb
+            cb.finalize(self.object_prediction if alg is None else alg.object_prediction)
 
     def compute_uncertainty(self, mask: torch.Tensor, data_storage_callbacks,
                             subiteration_number: int | None = None, return_pct: bool = False,

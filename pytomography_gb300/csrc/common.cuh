@@ -46,6 +46,40 @@ void clear_error();
 
 inline cudaStream_t as_stream(gb_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Host-side fault injection (tests of the error paths without a GPU fault).  A site armed
+// with a countdown n makes its n-th check from then on report a failure, once; sites are
+// armed by gb_inject_fault() or, at the first check, by the environment variable
+// GBTOMO_INJECT ("alloc:1", "launch:2,arg:1", ...).
+enum FaultSite { FAULT_ALLOC = 0, FAULT_LAUNCH = 1, FAULT_ARG = 2, FAULT_SITES = 3 };
+bool fault_injected(FaultSite site);
+
+// cudaMalloc with the allocation fault site in front of it.
+inline cudaError_t dev_alloc(void **p, size_t bytes) {
+    if (fault_injected(FAULT_ALLOC)) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+template <typename T>
+inline cudaError_t dev_alloc(T **p, size_t bytes) {
+    return dev_alloc(reinterpret_cast<void **>(p), bytes);
+}
+
+// Entry-point checks of the launch and argument fault sites: set the error message and
+// return the status the real failure would return.
+#define GB_INJECT_LAUNCH()                                                  \
+    do {                                                                    \
+        if (::gb::fault_injected(::gb::FAULT_LAUNCH)) {                     \
+            ::gb::set_error("kernel launch failed: injected launch failure"); \
+            return GB_ERR_CUDA;                                             \
+        }                                                                   \
+    } while (0)
+#define GB_INJECT_ARG()                                             \
+    do {                                                            \
+        if (::gb::fault_injected(::gb::FAULT_ARG)) {                \
+            ::gb::set_error("invalid argument: injected bad argument"); \
+            return GB_ERR_ARG;                                      \
+        }                                                           \
+    } while (0)
+
 int device_sm_count();
 
 }  // namespace gb

@@ -210,7 +210,7 @@ static gb_status build_tiles(gb_pet_plan *p, int n_subsets) {
         for (int s = 0; s < n_subsets; s++) p->list_off.push_back(0);
         return GB_OK;
     }
-    GB_CUDA(cudaMalloc(&p->d_rec, (size_t)(2 * E) * sizeof(int4)));
+    GB_CUDA(dev_alloc(&p->d_rec, (size_t)(2 * E) * sizeof(int4)));
     unsigned *keys = nullptr, *keys2 = nullptr;
     int *vals = nullptr, *vals2 = nullptr;
     void *tmp = nullptr;
@@ -221,14 +221,14 @@ static gb_status build_tiles(gb_pet_plan *p, int n_subsets) {
         set_error("event tile build failed: %s", cudaGetErrorString(err));
         return err == cudaErrorMemoryAllocation ? GB_ERR_OOM : GB_ERR_CUDA;
     };
-    if ((e = cudaMalloc(&keys, E * sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&keys2, E * sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&vals, E * sizeof(int))) != cudaSuccess ||
-        (e = cudaMalloc(&vals2, E * sizeof(int))) != cudaSuccess)
+    if ((e = dev_alloc(&keys, E * sizeof(unsigned))) != cudaSuccess ||
+        (e = dev_alloc(&keys2, E * sizeof(unsigned))) != cudaSuccess ||
+        (e = dev_alloc(&vals, E * sizeof(int))) != cudaSuccess ||
+        (e = dev_alloc(&vals2, E * sizeof(int))) != cudaSuccess)
         return fail(e);
     if ((e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, vals2,
                                              (int)E, 0, 23)) != cudaSuccess ||
-        (e = cudaMalloc(&tmp, tmp_bytes)) != cudaSuccess)
+        (e = dev_alloc(&tmp, tmp_bytes)) != cudaSuccess)
         return fail(e);
     long long off = 0;
     for (int li = 0; li <= n_subsets; li++) {
@@ -290,7 +290,7 @@ gb_status gb_pet_plan_create(const gb_pet_desc *d, gb_pet_plan **out) {
     p->n_events = d->n_events;
     p->img_size = (long long)d->nx * d->ny * d->nz;
     cudaError_t e;
-    if ((e = cudaMalloc(&p->d_lut, (size_t)d->n_det * 3 * sizeof(float))) != cudaSuccess ||
+    if ((e = dev_alloc(&p->d_lut, (size_t)d->n_det * 3 * sizeof(float))) != cudaSuccess ||
         (e = cudaMemcpy(p->d_lut, d->lut, (size_t)d->n_det * 3 * sizeof(float),
                         cudaMemcpyHostToDevice)) != cudaSuccess) {
         set_error("LUT upload failed: %s", cudaGetErrorString(e));
@@ -303,7 +303,7 @@ gb_status gb_pet_plan_create(const gb_pet_desc *d, gb_pet_plan **out) {
         std::vector<float> tab;
         float inv_step = 0.f;
         tof_weight_table(d->tof_bin_width, d->tof_sigma, d->tof_n_sigmas, tab, inv_step);
-        if ((e = cudaMalloc(&p->d_tof_tab, tab.size() * sizeof(float))) != cudaSuccess ||
+        if ((e = dev_alloc(&p->d_tof_tab, tab.size() * sizeof(float))) != cudaSuccess ||
             (e = cudaMemcpy(p->d_tof_tab, tab.data(), tab.size() * sizeof(float),
                             cudaMemcpyHostToDevice)) != cudaSuccess) {
             set_error("TOF table upload failed: %s", cudaGetErrorString(e));
@@ -315,10 +315,10 @@ gb_status gb_pet_plan_create(const gb_pet_desc *d, gb_pet_plan **out) {
     }
     if (d->n_events > 0) {
         size_t bytes = (size_t)d->n_events * p->ncol * sizeof(int);
-        if ((e = cudaMalloc(&p->d_ev, bytes)) != cudaSuccess ||
+        if ((e = dev_alloc(&p->d_ev, bytes)) != cudaSuccess ||
             (e = cudaMemcpy(p->d_ev, d->events, bytes, cudaMemcpyDefault)) != cudaSuccess ||
-            (e = cudaMalloc(&p->d_ratio, (size_t)d->n_events * sizeof(float))) != cudaSuccess ||
-            (e = cudaMalloc(&p->d_bp, (size_t)p->img_size * sizeof(float))) != cudaSuccess) {
+            (e = dev_alloc(&p->d_ratio, (size_t)d->n_events * sizeof(float))) != cudaSuccess ||
+            (e = dev_alloc(&p->d_bp, (size_t)p->img_size * sizeof(float))) != cudaSuccess) {
             set_error("event upload failed: %s", cudaGetErrorString(e));
             pet_free(p);
             return e == cudaErrorMemoryAllocation ? GB_ERR_OOM : GB_ERR_CUDA;
@@ -366,8 +366,10 @@ gb_status gb_pet_set_subsets(gb_pet_plan *p, int32_t n_subsets) {
 gb_status gb_pet_forward(gb_pet_plan *p, const float *img, float *proj, int32_t subset,
                          gb_stream_t stream) {
     clear_error();
+    GB_INJECT_ARG();
     GB_CHECK_ARG(p && img && proj, "null argument");
     GB_CHECK_ARG(subset < p->n_subsets, "subset out of range");
+    GB_INJECT_LAUNCH();
     long long first, stride, n;
     subset_range(p, subset, first, stride, n);
     if (n == 0) return GB_OK;
@@ -386,8 +388,10 @@ gb_status gb_pet_forward(gb_pet_plan *p, const float *img, float *proj, int32_t 
 gb_status gb_pet_backward(gb_pet_plan *p, const float *proj, float *img, int32_t subset,
                           gb_stream_t stream) {
     clear_error();
+    GB_INJECT_ARG();
     GB_CHECK_ARG(p && img && proj, "null argument");
     GB_CHECK_ARG(((uintptr_t)img & 15) == 0, "image buffer must be 16-byte aligned");
+    GB_INJECT_LAUNCH();
     GB_CHECK_ARG(subset < p->n_subsets, "subset out of range");
     long long first, stride, n;
     subset_range(p, subset, first, stride, n);
@@ -408,7 +412,9 @@ gb_status gb_pet_osem_step(gb_pet_plan *p, float *img, const float *numerator,
                            int64_t numerator_len, const float *additive, const float *norm_bp,
                            int32_t subset, gb_stream_t stream) {
     clear_error();
+    GB_INJECT_ARG();
     GB_CHECK_ARG(p && img && numerator && norm_bp, "null argument");
+    GB_INJECT_LAUNCH();
     GB_CHECK_ARG(numerator_len == 1 || numerator_len == p->n_events,
                  "numerator must hold 1 or n_events values");
     GB_CHECK_ARG(subset < p->n_subsets, "subset out of range");

@@ -175,10 +175,10 @@ gb_status gb_pet_sino_plan_create(const gb_pet_sino_desc *d, gb_pet_sino_plan **
     p->geom.P = d->n_planes;
     const size_t ndet = (size_t)d->n_angles * d->n_radial * 4, nz2 = (size_t)d->n_planes * 2;
     cudaError_t e;
-    if ((e = cudaMalloc(&p->d_det, ndet * sizeof(float))) != cudaSuccess ||
+    if ((e = dev_alloc(&p->d_det, ndet * sizeof(float))) != cudaSuccess ||
         (e = cudaMemcpy(p->d_det, d->det_xy, ndet * sizeof(float), cudaMemcpyHostToDevice)) !=
             cudaSuccess ||
-        (e = cudaMalloc(&p->d_z, nz2 * sizeof(float))) != cudaSuccess ||
+        (e = dev_alloc(&p->d_z, nz2 * sizeof(float))) != cudaSuccess ||
         (e = cudaMemcpy(p->d_z, d->plane_z, nz2 * sizeof(float), cudaMemcpyHostToDevice)) !=
             cudaSuccess) {
         set_error("sinogram table upload failed: %s", cudaGetErrorString(e));
@@ -191,7 +191,7 @@ gb_status gb_pet_sino_plan_create(const gb_pet_sino_desc *d, gb_pet_sino_plan **
         std::vector<float> tab;
         float inv_step = 0.f;
         tof_weight_table(d->tof_bin_width, d->tof_sigma, d->tof_n_sigmas, tab, inv_step);
-        if ((e = cudaMalloc(&p->d_tof_tab, tab.size() * sizeof(float))) != cudaSuccess ||
+        if ((e = dev_alloc(&p->d_tof_tab, tab.size() * sizeof(float))) != cudaSuccess ||
             (e = cudaMemcpy(p->d_tof_tab, tab.data(), tab.size() * sizeof(float),
                             cudaMemcpyHostToDevice)) != cudaSuccess) {
             set_error("TOF table upload failed: %s", cudaGetErrorString(e));

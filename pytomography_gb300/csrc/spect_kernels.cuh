@@ -44,7 +44,12 @@ struct SpectDev {
     int psf;                // PSF present
     int psf2d;              // PSF blurs z as well
     unsigned long long *phase;  // diagnostic builds: per-CTA forward phase cycles, or null
+    unsigned wait_polls;        // polls of a bounded mbarrier wait before it gives up
+    int dbg_skip_first_copy;    // test hook: the forward never issues its first TMA copy
 };
+
+// Polls of a bounded wait (each suspends for at most 20 us): about 1.3 s.
+constexpr unsigned kWaitPolls = 1u << 16;
 
 // Epilogue of the gather back-projector.
 enum B2Mode : int {

@@ -1,7 +1,10 @@
 // C ABI of the SPECT projector: plan creation (tables, attenuation precompute,
 // scratch), subset bookkeeping and the stream-ordered projector / update calls.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
+#include <mutex>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -23,6 +26,44 @@ void set_error(const char *fmt, ...) {
     g_err = buf;
 }
 void clear_error() { g_err.clear(); }
+
+// ---------------------------------------------------------------- fault injection
+static std::atomic<int> g_fault_countdown[FAULT_SITES];
+static std::once_flag g_fault_env_once;
+
+static int fault_site_of(const std::string &name) {
+    if (name == "alloc") return FAULT_ALLOC;
+    if (name == "launch") return FAULT_LAUNCH;
+    if (name == "arg") return FAULT_ARG;
+    return -1;
+}
+
+// GBTOMO_INJECT="site:n[,site:n...]" arms the sites at the first check of the process.
+static void fault_env_init() {
+    const char *env = std::getenv("GBTOMO_INJECT");
+    if (!env) return;
+    std::string spec(env);
+    size_t pos = 0;
+    while (pos < spec.size()) {
+        size_t end = spec.find(',', pos);
+        if (end == std::string::npos) end = spec.size();
+        const std::string item = spec.substr(pos, end - pos);
+        const size_t colon = item.find(':');
+        const int site = fault_site_of(item.substr(0, colon));
+        const int n = colon == std::string::npos ? 1 : std::atoi(item.c_str() + colon + 1);
+        if (site >= 0 && n > 0) g_fault_countdown[site].store(n);
+        pos = end + 1;
+    }
+}
+
+bool fault_injected(FaultSite site) {
+    std::call_once(g_fault_env_once, fault_env_init);
+    int c = g_fault_countdown[site].load();
+    while (c > 0) {
+        if (g_fault_countdown[site].compare_exchange_weak(c, c - 1)) return c == 1;
+    }
+    return false;
+}
 
 int device_sm_count() {
     int dev = 0, n = 0;
@@ -304,20 +345,20 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
     p->d_alist = nullptr;
     p->d_items = nullptr;
     p->d_ioff = nullptr;
-    GB_CUDA(cudaMalloc(&p->d_alist, all.size() * sizeof(int)));
+    GB_CUDA(dev_alloc(&p->d_alist, all.size() * sizeof(int)));
     GB_CUDA(cudaMemcpy(p->d_alist, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMalloc(&p->d_items, std::max<size_t>(1, items.size()) * sizeof(int4)));
+    GB_CUDA(dev_alloc(&p->d_items, std::max<size_t>(1, items.size()) * sizeof(int4)));
     if (!items.empty())
         GB_CUDA(cudaMemcpy(p->d_items, items.data(), items.size() * sizeof(int4),
                            cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMalloc(&p->d_ioff, ioff.size() * sizeof(int)));
+    GB_CUDA(dev_alloc(&p->d_ioff, ioff.size() * sizeof(int)));
     GB_CUDA(cudaMemcpy(p->d_ioff, ioff.data(), ioff.size() * sizeof(int), cudaMemcpyHostToDevice));
     p->n_subsets = n_subsets;
     size_t need = max_items * p->N * p->nz;
     if (need > p->partials_cap) {
         cudaFree(p->d_partials);
         p->d_partials = nullptr;
-        GB_CUDA(cudaMalloc(&p->d_partials, need * sizeof(float)));
+        GB_CUDA(dev_alloc(&p->d_partials, need * sizeof(float)));
         p->partials_cap = need;
     }
     return GB_OK;
@@ -369,6 +410,17 @@ static int choose_zt(int K, int N, int nz, bool fwd, int tpb = 512) {
 extern "C" {
 
 const char *gb_last_error(void) { return g_err.c_str(); }
+
+gb_status gb_inject_fault(const char *site, int32_t nth) {
+    clear_error();
+    std::call_once(g_fault_env_once, fault_env_init);
+    GB_CHECK_ARG(site, "null site");
+    const int s = fault_site_of(site);
+    GB_CHECK_ARG(s >= 0, "unknown fault site '%s' (alloc, launch, arg)", site);
+    GB_CHECK_ARG(nth >= 0, "nth must be >= 0");
+    g_fault_countdown[s].store(nth);
+    return GB_OK;
+}
 const char *gb_version(void) { return "gbtomo 0.1.0 (sm_103a)"; }
 
 gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
@@ -436,6 +488,8 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     g.psf = psf;
     g.att_first = att && (!psf || order == "ap");
     g.psf2d = psf ? (d->psf_2d ? 1 : 0) : 0;
+    g.wait_polls = kWaitPolls;
+    g.dbg_skip_first_copy = 0;
 
 #define FAIL_CUDA(call)                                                                   \
     do {                                                                                  \
@@ -450,16 +504,16 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     const int n = d->n_angles, Lp = p->Lp;
     p->h_theta_fwd.assign(d->theta_fwd, d->theta_fwd + 6 * n);
     p->h_lin.assign(d->lin, d->lin + Lp);
-    FAIL_CUDA(cudaMalloc(&p->d_lin, Lp * sizeof(float)));
+    FAIL_CUDA(dev_alloc(&p->d_lin, Lp * sizeof(float)));
     FAIL_CUDA(cudaMemcpy(p->d_lin, d->lin, Lp * sizeof(float), cudaMemcpyHostToDevice));
-    FAIL_CUDA(cudaMalloc(&p->d_theta_fwd, 6 * n * sizeof(float)));
+    FAIL_CUDA(dev_alloc(&p->d_theta_fwd, 6 * n * sizeof(float)));
     FAIL_CUDA(cudaMemcpy(p->d_theta_fwd, d->theta_fwd, 6 * n * sizeof(float), cudaMemcpyHostToDevice));
-    FAIL_CUDA(cudaMalloc(&p->d_theta_bwd, 6 * n * sizeof(float)));
+    FAIL_CUDA(dev_alloc(&p->d_theta_bwd, 6 * n * sizeof(float)));
     FAIL_CUDA(cudaMemcpy(p->d_theta_bwd, d->theta_bwd, 6 * n * sizeof(float), cudaMemcpyHostToDevice));
     std::vector<int> grp(n, 0);
     if (psf) std::copy(d->psf_group, d->psf_group + n, grp.begin());
     p->h_group = grp;
-    FAIL_CUDA(cudaMalloc(&p->d_group, n * sizeof(int)));
+    FAIL_CUDA(dev_alloc(&p->d_group, n * sizeof(int)));
     FAIL_CUDA(cudaMemcpy(p->d_group, grp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     if (psf) {
         // centre the caller's k taps inside K, drop taps below psf_trunc_rel * row max
@@ -497,11 +551,11 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
                 tier[(size_t)gi * Lp + x] = (signed char)t;
             }
         p->h_tier = tier;
-        FAIL_CUDA(cudaMalloc(&p->d_tier, tier.size()));
+        FAIL_CUDA(dev_alloc(&p->d_tier, tier.size()));
         FAIL_CUDA(cudaMemcpy(p->d_tier, tier.data(), tier.size(), cudaMemcpyHostToDevice));
-        FAIL_CUDA(cudaMalloc(&p->d_taps_r, tr.size() * sizeof(float)));
+        FAIL_CUDA(dev_alloc(&p->d_taps_r, tr.size() * sizeof(float)));
         FAIL_CUDA(cudaMemcpy(p->d_taps_r, tr.data(), tr.size() * sizeof(float), cudaMemcpyHostToDevice));
-        FAIL_CUDA(cudaMalloc(&p->d_taps_z, tz.size() * sizeof(float)));
+        FAIL_CUDA(dev_alloc(&p->d_taps_z, tz.size() * sizeof(float)));
         FAIL_CUDA(cudaMemcpy(p->d_taps_z, tz.data(), tz.size() * sizeof(float), cudaMemcpyHostToDevice));
         p->Zt_fwd = choose_zt(K, p->N, p->nz, true);
         p->Zt_b1 = choose_zt(K, p->N, p->nz, false);
@@ -525,19 +579,19 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     g.tier = p->d_tier;
     if (att) {
         size_t na = (size_t)n * Lp * g.nya * p->nz;
-        FAIL_CUDA(cudaMalloc(&p->d_A, na * sizeof(float)));
+        FAIL_CUDA(dev_alloc(&p->d_A, na * sizeof(float)));
         g.A = p->d_A;
         FAIL_CUDA(launch_atten(g, d->mu, d->dx, n, p->d_A, 0));
         FAIL_CUDA(cudaStreamSynchronize(0));
     }
     // scratch: W for one angle group, likelihood ratio of all angles, multi-group bp
     p->G = std::min(n, 16);
-    FAIL_CUDA(cudaMalloc(&p->d_W, (size_t)p->G * Lp * g.nya * p->nz * sizeof(float)));
-    FAIL_CUDA(cudaMalloc(&p->d_ratio, (size_t)n * p->N * p->nz * sizeof(float)));
-    FAIL_CUDA(cudaMalloc(&p->d_bp, (size_t)p->N * p->N * p->nz * sizeof(float)));
-    FAIL_CUDA(cudaMalloc(&p->d_wrange, (size_t)p->G * Lp * sizeof(int2)));
+    FAIL_CUDA(dev_alloc(&p->d_W, (size_t)p->G * Lp * g.nya * p->nz * sizeof(float)));
+    FAIL_CUDA(dev_alloc(&p->d_ratio, (size_t)n * p->N * p->nz * sizeof(float)));
+    FAIL_CUDA(dev_alloc(&p->d_bp, (size_t)p->N * p->N * p->nz * sizeof(float)));
+    FAIL_CUDA(dev_alloc(&p->d_wrange, (size_t)p->G * Lp * sizeof(int2)));
     FAIL_CUDA(cudaMemset(p->d_wrange, 0, (size_t)p->G * Lp * sizeof(int2)));
-    FAIL_CUDA(cudaMalloc(&p->d_err, sizeof(int)));
+    FAIL_CUDA(dev_alloc(&p->d_err, sizeof(int)));
     FAIL_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
     g.wrange = p->d_wrange;
     g.err = p->d_err;
@@ -564,6 +618,22 @@ gb_status gb_spect_device_status(gb_spect_plan *p, int32_t *code) {
     clear_error();
     GB_CHECK_ARG(p && code, "null argument");
     GB_CUDA(cudaMemcpy(code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    return GB_OK;
+}
+
+gb_status gb_spect_clear_device_status(gb_spect_plan *p) {
+    clear_error();
+    GB_CHECK_ARG(p, "null plan");
+    GB_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+    return GB_OK;
+}
+
+gb_status gb_spect_set_debug(gb_spect_plan *p, int32_t skip_first_copy, int32_t wait_polls) {
+    clear_error();
+    GB_CHECK_ARG(p, "null plan");
+    GB_CHECK_ARG(wait_polls >= 0, "wait_polls must be >= 0");
+    p->dev.dbg_skip_first_copy = skip_first_copy ? 1 : 0;
+    p->dev.wait_polls = wait_polls ? (unsigned)wait_polls : kWaitPolls;
     return GB_OK;
 }
 
@@ -675,7 +745,9 @@ static gb_status run_forward(gb_spect_plan *p, const float *obj, int subset, flo
 gb_status gb_spect_forward(gb_spect_plan *p, const float *obj, float *proj, int32_t subset,
                            gb_stream_t stream) {
     clear_error();
+    GB_INJECT_ARG();
     GB_CHECK_ARG(p && obj && proj, "null argument");
+    GB_INJECT_LAUNCH();
     return run_forward(p, obj, subset, proj, 0, nullptr, nullptr, nullptr, as_stream(stream));
 }
 
@@ -714,7 +786,9 @@ static gb_status run_backward(gb_spect_plan *p, const float *proj, int li, int a
 gb_status gb_spect_backward(gb_spect_plan *p, const float *proj, float *obj, int32_t subset,
                             int32_t adjoint, gb_stream_t stream) {
     clear_error();
+    GB_INJECT_ARG();
     GB_CHECK_ARG(p && proj && obj, "null argument");
+    GB_INJECT_LAUNCH();
     const int li = list_index(p, subset);
     if (li < 0) {
         set_error("subset %d out of range (n_subsets=%d)", subset, p->n_subsets);
@@ -764,9 +838,9 @@ gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
             return e_ == cudaErrorMemoryAllocation ? GB_ERR_OOM : GB_ERR_CUDA;         \
         }                                                                              \
     } while (0)
-    TUNE_CUDA(cudaMalloc(&obj, vol * sizeof(float)));
-    TUNE_CUDA(cudaMalloc(&proj, npr * sizeof(float)));
-    TUNE_CUDA(cudaMalloc(&back, vol * sizeof(float)));
+    TUNE_CUDA(dev_alloc(&obj, vol * sizeof(float)));
+    TUNE_CUDA(dev_alloc(&proj, npr * sizeof(float)));
+    TUNE_CUDA(dev_alloc(&back, vol * sizeof(float)));
     {
         std::vector<float> ones(vol, 1.0f);
         TUNE_CUDA(cudaMemcpy(obj, ones.data(), vol * sizeof(float), cudaMemcpyHostToDevice));
@@ -850,7 +924,9 @@ gb_status gb_spect_osem_step(gb_spect_plan *p, float *obj, const float *g, const
                              const float *nbp, int32_t subset, float *pred,
                              gb_stream_t stream) {
     clear_error();
+    GB_INJECT_ARG();
     GB_CHECK_ARG(p && obj && g && nbp, "null argument");
+    GB_INJECT_LAUNCH();
     cudaStream_t st = as_stream(stream);
     gb_status r = run_forward(p, obj, subset, p->d_ratio, 1, g, s, pred, st);
     if (r != GB_OK) return r;
@@ -879,6 +955,7 @@ gb_status gb_spect_bsrem_step(gb_spect_plan *p, const float *in, float *out, con
     clear_error();
     GB_CHECK_ARG(p && in && out && g && nbp && nbp_sum, "null argument");
     GB_CHECK_ARG(in != out, "BSREM needs distinct input and output objects");
+    GB_INJECT_LAUNCH();
     cudaStream_t st = as_stream(stream);
     gb_status r = run_forward(p, in, subset, p->d_ratio, 1, g, s, nullptr, st);
     if (r != GB_OK) return r;
@@ -928,7 +1005,7 @@ extern "C" int gb_debug_fwd_phase_cycles(gb_spect_plan *p, unsigned long long *o
 }
 extern "C" int gb_debug_fwd_phase_reset(gb_spect_plan *p) {
     if (!p->dev.phase) {
-        cudaError_t e = cudaMalloc(&p->dev.phase, sizeof(unsigned long long) * 4096 * 16);
+        cudaError_t e = dev_alloc(&p->dev.phase, sizeof(unsigned long long) * 4096 * 16);
         if (e != cudaSuccess) return (int)e;
     }
     return (int)cudaMemset(p->dev.phase, 0, sizeof(unsigned long long) * 4096 * 16);

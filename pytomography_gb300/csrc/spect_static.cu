@@ -1,10 +1,10 @@
 // Forward projection that allocates nothing: its cross-chunk partial sums live in a
 // fixed file-scope device array instead of the plan's scratch buffer.
 //
-// Who needs it: callers that must not allocate device memory while they run — code
-// executing under a CUDA-graph capture or a stream-ordered memory pool that forbids
-// cudaMalloc, host processes whose device memory is owned by another framework's
-// allocator, or long-running services that budget every allocation up front.  They
+// Who needs it: callers that must not allocate device memory while they run — code on a
+// stream whose memory pool forbids further cudaMalloc, host processes whose device memory
+// is owned by another framework's allocator, or long-running services that budget every
+// allocation up front.  They
 // create their plan once at set-up; afterwards this entry point touches only the plan's
 // read-only tables, the caller's input and output, and the static array below.
 //

@@ -34,6 +34,8 @@ class SPECTSystemMatrix(SystemMatrix):
             change (results are cached per geometry for the process) instead of using the
             shared-memory-derived defaults.  Tiles change no result beyond the order of
             floating-point sums.
+        check_device_status: after every projector call, read the plan's device error
+            word (a synchronous read) and raise if a kernel gave up on a bounded wait.
     """
 
     _tuning_cache: dict = {}
@@ -41,13 +43,14 @@ class SPECTSystemMatrix(SystemMatrix):
     def __init__(self, obj2obj_transforms, proj2proj_transforms, object_meta, proj_meta,
                  object_initial_based_on_camera_path: bool = False,
                  psf_trunc_rel: float = 1e-7, autotune: bool = False,
-                 _no_pad: bool = False) -> None:
+                 check_device_status: bool = False, _no_pad: bool = False) -> None:
         if proj2proj_transforms:
             raise NotImplementedError("proj2proj transforms are not part of the fused path")
         super().__init__(object_meta, proj_meta, obj2obj_transforms, proj2proj_transforms)
         self.object_initial_based_on_camera_path = object_initial_based_on_camera_path
         self.psf_trunc_rel = float(psf_trunc_rel)
         self.autotune_enabled = bool(autotune)
+        self.check_device_status = bool(check_device_status)
         self._no_pad = bool(_no_pad)  # unpadded rotation frame (the StarGuide projector)
         self._plan = None
         self._lib = _lib.load()
@@ -164,6 +167,20 @@ class SPECTSystemMatrix(SystemMatrix):
         _lib.check(self._lib.gb_spect_device_status(self._plan, ctypes.byref(code)))
         return int(code.value)
 
+    def raise_on_device_error(self) -> None:
+        """Raise (and reset the error word) when a kernel of this plan gave up on a
+        bounded wait; its outputs since the last check are then invalid."""
+        code = self.device_status()
+        if code:
+            _lib.check(self._lib.gb_spect_clear_device_status(self._plan))
+            raise RuntimeError(f"gbtomo device error {code}: a projector kernel gave up waiting "
+                               "for its attenuation copies; outputs since the last check are "
+                               "invalid")
+
+    def _after_call(self) -> None:
+        if self.check_device_status:
+            self.raise_on_device_error()
+
     # ------------------------------------------------------------ subsets
     def set_n_subsets(self, n_subsets: int) -> None:
         indices = torch.arange(self.proj_meta.shape[0]).to(torch.long).to(self.device)
@@ -245,6 +262,7 @@ class SPECTSystemMatrix(SystemMatrix):
                           device=self.device, dtype=torch.float32)
         _lib.check(self._lib.gb_spect_forward(self._plan, _lib.ptr(obj), _lib.ptr(out), code,
                                               _lib.stream_handle(self.device)))
+        self._after_call()
         return out
 
     def _backward(self, proj: torch.Tensor, subset_idx, adjoint: int) -> torch.Tensor:
@@ -256,6 +274,7 @@ class SPECTSystemMatrix(SystemMatrix):
         out = torch.empty(tuple(self.object_meta.shape), device=self.device, dtype=torch.float32)
         _lib.check(self._lib.gb_spect_backward(self._plan, _lib.ptr(p), _lib.ptr(out), code,
                                                adjoint, _lib.stream_handle(self.device)))
+        self._after_call()
         return out
 
     def backward(self, proj: torch.Tensor, subset_idx: int | None = None) -> torch.Tensor:
@@ -283,6 +302,7 @@ class SPECTSystemMatrix(SystemMatrix):
         _lib.check(self._lib.gb_spect_osem_step(
             self._plan, _lib.ptr(object), _lib.ptr(g), _lib.ptr(s), _lib.ptr(nb),
             self._subset_code(subset_idx), _lib.ptr(predicted), _lib.stream_handle(self.device)))
+        self._after_call()
 
     def bsrem_step(self, object_in, object_out, projections, additive, norm_bp, norm_bp_sum,
                    relax: float, subset_weight: float, prior=None, floor_value: float = 1e-4,

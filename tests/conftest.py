@@ -45,3 +45,20 @@ def cuda():
     from pytomography_gb300 import _lib
     _lib.load()
     return torch.device("cuda")
+
+
+# Relative L2 errors against the float64 oracle recorded by the full-size parity tests,
+# printed in the terminal summary so that every run states them per configuration.
+PARITY_REPORT: dict = {}
+
+
+def report_parity(name: str, value: float) -> None:
+    PARITY_REPORT[name] = max(float(value), PARITY_REPORT.get(name, 0.0))
+
+
+def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    if not PARITY_REPORT:
+        return
+    terminalreporter.section("relative L2 vs the float64 oracle (max over the checked items)")
+    for k in sorted(PARITY_REPORT):
+        terminalreporter.write_line(f"{k}: {PARITY_REPORT[k]:.3e}")

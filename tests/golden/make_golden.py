@@ -1,8 +1,10 @@
 """Generate the golden fixtures under ``tests/golden/`` from the upstream code.
 
-Run in a container that holds the upstream PyTomography sources::
+Run in a container that holds the upstream PyTomography sources, with
+``PYTOMOGRAPHY_REFERENCE_SRC`` naming their ``src`` folder::
 
-    python tests/golden/make_golden.py            # writes tests/golden/*.npz
+    python tests/golden/make_golden.py            # writes every tests/golden/*.npz
+    python tests/golden/make_golden.py plugins    # writes only the named cases
 
 Every output in the fixtures is produced by the upstream implementation itself
 (``SPECTSystemMatrix.forward/backward``, ``SPECTAttenuationTransform``,
@@ -458,8 +460,63 @@ def autograd_case(out):
     print("wrote autograd")
 
 
+def plugins_case(out):
+    """The two obj2obj plugins called on their own, one projection index at a time, on
+    seeded objects already in the detector frame (SPECTAttenuationTransform.forward /
+    backward, attenuation.py:72-115; SPECTPSFTransform.forward / backward, psf.py:199-231),
+    in the padded frame of SPECTSystemMatrix and in the unpadded frame
+    (assume_padded=False) of the StarGuide system matrix."""
+    shape, dr = (14, 14, 8), (0.45, 0.45, 0.5)
+    angles = [0.0, 33.0, 90.0, 145.5, 200.0, 271.0, 318.0]
+    radii = [21.0, 25.0, 21.0, 23.0, 25.0, 21.0, 24.5]
+    f_np, mu_np = ellipsoid_phantom(shape, dr, seed=31)
+    rng = np.random.default_rng(32)
+    pad = compute_pad_size(shape[0])
+    L = shape[0] + 2 * pad
+    rec = {"shape": np.array(shape), "dr": np.array(dr), "angles": np.array(angles),
+           "radii": np.array(radii), "mu": mu_np, "pad": pad}
+    x_pad = (rng.random((L, L, shape[2])) * 4).astype(np.float32)
+    x_unp = (rng.random(shape) * 4).astype(np.float32)
+    rec["x_padded"], rec["x_unpadded"] = x_pad, x_unp
+    idx = [0, 3, 5]
+    rec["indices"] = np.array(idx)
+    for prec, dt in (("f32", torch.float32), ("f64", torch.float64)):
+        set_precision(dt)
+        om = SPECTObjectMeta(list(dr), tuple(shape))
+        pm = SPECTProjMeta((shape[1], shape[2]), list(dr[:2]), list(angles), radii=list(radii))
+        for frame, x_np, padded in (("pad", x_pad, True), ("unpad", x_unp, False)):
+            att = SPECTAttenuationTransform(torch.tensor(mu_np, dtype=dt), assume_padded=padded)
+            psf2 = SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)), assume_padded=padded)
+            psf1 = SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11), kernel_dimensions="1D"),
+                                     assume_padded=padded)
+            for t in (att, psf2, psf1):
+                t.configure(om, pm)
+            x = torch.tensor(x_np, dtype=dt)
+            for i in idx:
+                ai = torch.tensor(i)
+                outs = {"att_fwd": att.forward(x, ai), "att_bwd": att.backward(x, ai),
+                        "psf_fwd": psf2.forward(x, ai), "psf_bwd": psf2.backward(x, ai),
+                        "psf1d_fwd": psf1.forward(x, ai)}
+                for k, v in outs.items():
+                    if prec == "f64" and (frame != "pad" or k.endswith("bwd")):
+                        continue
+                    rec[f"{k.replace('_', '_' + frame + '_', 1)}_{i}_{prec}"] = v.detach().numpy()
+    set_precision(torch.float32)
+    np.savez_compressed(os.path.join(out, "plugins.npz"), **rec)
+    print("wrote plugins", L)
+
+
+CASES = {}
+
+
 def main():
     out = HERE
+    only = set(sys.argv[1:])
+    if only:
+        for name in sorted(only):
+            {"plugins": plugins_case}[name](out)
+        return
+    plugins_case(out)
     autograd_case(out)
     theta_case(out)
     torch.manual_seed(0)

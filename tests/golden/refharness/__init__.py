@@ -36,7 +36,8 @@ import types
 import torch
 import torch.nn.functional as F
 
-REFERENCE_SRC = os.environ.get("PYTOMOGRAPHY_REFERENCE_SRC", "/root/reference/src")
+# the upstream ``src`` folder (the one holding the ``pytomography`` package); no default
+REFERENCE_SRC = os.environ.get("PYTOMOGRAPHY_REFERENCE_SRC", "")
 
 _ABSENT = (
     "pydicom", "rt_utils", "nibabel", "pandas", "h5py", "uproot", "torchrbf",
@@ -174,8 +175,9 @@ def install():
     global _installed
     if _installed:
         return
-    if not os.path.isdir(os.path.join(REFERENCE_SRC, "pytomography")):
-        raise RuntimeError(f"upstream sources not found under {REFERENCE_SRC}")
+    if not REFERENCE_SRC or not os.path.isdir(os.path.join(REFERENCE_SRC, "pytomography")):
+        raise RuntimeError("set PYTOMOGRAPHY_REFERENCE_SRC to the upstream src folder "
+                           f"(got {REFERENCE_SRC!r})")
     sys.meta_path.insert(0, _PlaceholderFinder())
     real_version = importlib.metadata.version
 

@@ -80,3 +80,23 @@ def test_rdp_oracle_matches_reference():
 
 def test_pad_sizes():
     assert [oracle.pad_size(n) for n in (15, 16, 64, 96, 128)] == [4, 4, 14, 20, 27]
+
+
+def test_oracle_plugins_match_reference_plugins():
+    """orc_spect_plugin (attenuation and PSF on a detector-frame object) against the
+    reference's own SPECTAttenuationTransform / SPECTPSFTransform calls."""
+    d = golden("plugins")
+    dr = d["dr"]
+    for i in (int(v) for v in d["indices"]):
+        beta, r = float(d["angles"][i]), float(d["radii"][i])
+        xp = d["x_padded"].astype(np.float64)
+        xu = d["x_unpadded"].astype(np.float64)
+        a = oracle.spect_plugin("att", xp, dr, beta, mu=d["mu"])
+        assert rel_l2(a, d[f"att_pad_fwd_{i}_f64"]) < 1e-12
+        assert rel_l2(a, d[f"att_pad_fwd_{i}_f32"]) < 1e-6
+        a = oracle.spect_plugin("att", xu, dr, beta, mu=d["mu"], pad=0)
+        assert rel_l2(a, d[f"att_unpad_fwd_{i}_f32"]) < 1e-6
+        p = oracle.spect_plugin("psf", xp, dr, beta, psf=(0.03, 0.11), radius=r)
+        assert rel_l2(p, d[f"psf_pad_fwd_{i}_f64"]) < 1e-12
+        p = oracle.spect_plugin("psf", xu, dr, beta, psf=(0.03, 0.11), radius=r, psf_2d=False)
+        assert rel_l2(p, d[f"psf1d_unpad_fwd_{i}_f32"]) < 1e-6
