@@ -78,6 +78,8 @@ typedef struct gb_spect_desc {
     int32_t no_pad;           /* 1: rotate in the unpadded nx x nx frame (n_pad = nx), as the
                                  StarGuide system matrix does (transforms configured with
                                  assume_padded=False); 0: the padded frame of SPECTSystemMatrix */
+    int32_t psf_k_min;        /* 0, or a tap count the plan's PSF bucket must hold at least:
+                                 plans run together by gb_spect_batch_create share one bucket */
 } gb_spect_desc;
 
 /* Create / destroy a plan.  Creation uploads the geometry tables and precomputes the
@@ -199,6 +201,41 @@ gb_status gb_spect_attenuation_apply(const float *mu, int32_t n, int32_t nz, int
 gb_status gb_spect_psf_apply(const float *in, float *out, int32_t nplanes, int32_t ny,
                              int32_t nz, const float *taps_y, int32_t ky, const float *taps_z,
                              int32_t kz, gb_stream_t stream);
+
+/* ---------------------------------------------------------------- batches
+ * Several independent projection problems in one launch per phase: the reconstructions of
+ * a serving batch (each with its own plan: size, angles, attenuation, PSF), or several
+ * objects on one shared plan (a batch of the autograd path).  Replaces the reference's
+ * per-reconstruction, per-angle Python loops (projectors/SPECT/spect_system_matrix.py:
+ * 145-154, 188-198, driven by algorithms/preconditioned_gradient_ascent.py:80-129).
+ *
+ * A batch holds 1 to 32 entries, entry e projecting with plans[e] (plans may repeat).  The
+ * plans must have a PSF of one tap bucket (create them with a common psf_k_min), one
+ * subset count (subsets set before the batch is created), N <= 128, nz <= 128 and
+ * nz % 4 == 0.  The work items of every entry's angles are split by the plans' plane-cost
+ * model into about two waves of the GPU and dequeued, largest first, by one persistent CTA
+ * per SM; the per-(entry, angle) sums are reduced in plane order, so results do not depend
+ * on the queue order.  Creation allocates the batch's scratch (W stacks, ratio rows,
+ * partial sums); the calls allocate nothing.  Host arrays hold one device pointer per
+ * entry.  Calls on one batch must be ordered on one stream. */
+typedef struct gb_spect_batch gb_spect_batch;
+gb_status gb_spect_batch_create(gb_spect_plan *const *plans, int32_t n, gb_spect_batch **batch);
+gb_status gb_spect_batch_destroy(gb_spect_batch *batch);
+/* proj[e] [n_sel][ny][nz] = H_{e,m} objects[e] for every entry (subset -1: all angles). */
+gb_status gb_spect_batch_forward(gb_spect_batch *batch, const float *const *objects,
+                                 float *const *proj, int32_t subset, gb_stream_t stream);
+/* objects[e] (overwritten) = H_{e,m}^T proj[e]: adjoint = 0 the reference back-projector,
+ * 1 the exact transpose of gb_spect_batch_forward (objects 16-byte aligned). */
+gb_status gb_spect_batch_backward(gb_spect_batch *batch, const float *const *proj,
+                                  float *const *objects, int32_t subset, int32_t adjoint,
+                                  gb_stream_t stream);
+/* One fused OSEM sub-iteration of every entry, as gb_spect_osem_step with subset `subset`:
+ * objects[e] updated in place, projections[e] / additive[e] (additive may be NULL, or hold
+ * NULL entries) the full [n_angles][ny][nz] arrays, norm_bp[e] the entry's H_m^T 1. */
+gb_status gb_spect_batch_osem_step(gb_spect_batch *batch, float *const *objects,
+                                   const float *const *projections, const float *const *additive,
+                                   const float *const *norm_bp, int32_t subset,
+                                   gb_stream_t stream);
 
 /* Relative-difference prior with Euclidean neighbour weights
  * (priors/nearest_neighbour.py:156-183, 207-220). */

@@ -31,6 +31,7 @@ class SpectDesc(ctypes.Structure):
         ("psf_k", c_int), ("psf_taps_r", c_void_p), ("psf_taps_z", c_void_p),
         ("psf_trunc_rel", c_float),
         ("no_pad", c_int),
+        ("psf_k_min", c_int),
     ]
 
 
@@ -104,6 +105,12 @@ SIGNATURES = [
                                            c_void_p, c_void_p, c_void_p, c_void_p]),
     ("gb_spect_psf_apply", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int,
                                    c_void_p, c_int, c_void_p]),
+    ("gb_spect_batch_create", c_int, [c_void_p, c_int, ctypes.POINTER(c_void_p)]),
+    ("gb_spect_batch_destroy", c_int, [c_void_p]),
+    ("gb_spect_batch_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("gb_spect_batch_backward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    ("gb_spect_batch_osem_step", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                         c_void_p]),
     ("gb_rdp_gradient", c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_float,
                                 c_float, ctypes.POINTER(RdpDesc), c_float, c_void_p]),
     ("gb_rdp_hessian_vector", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_float,

@@ -143,17 +143,17 @@ __device__ __forceinline__ void st_vec(float *p, const float (&v)[OP]) {
 // o in [0, N+2H); input S rows i <-> padded y = pad-2H+i (projection rows at i in
 // [2H, 2H+N), zero elsewhere).
 // FIXED: N <= 128 and a z slab <= 128 wide: compile-time shared-memory strides.
+// One work item: planes [x0_, x1_) of angle ga (projection rows P, [N][nz]) for the z slab
+// at z0; writes the item's planes of the slot's W stack Ws ([Lp][nya][nz]) and row ranges
+// wr ([Lp]).  Called once per CTA by k_b1_psf and per dequeued item by the batch kernel.
 template <int K, bool VEC, bool FIXED>
-__global__ void __launch_bounds__(512, 1)
-    k_b1_psf(SpectDev g, const float *__restrict__ proj, const int *__restrict__ alist,
-             const int4 *__restrict__ items, int Zt, float *__restrict__ W) {
+__device__ __forceinline__ void b1_psf_item(const SpectDev &g, const float *__restrict__ P,
+                                            const int ga, int2 *__restrict__ wr, const int x0_,
+                                            const int x1_, const int z0, const int Zt,
+                                            float *__restrict__ Ws) {
     constexpr int H = K / 2;
     constexpr int OB = (K <= 31) ? 8 : 4;
-    const int4 item = items[blockIdx.x];  // (slot in group, first plane, end plane)
-    const int slot = item.x;
-    const int ga = alist[slot];
     const int N = g.N, nz = g.nz;
-    const int z0 = blockIdx.y * Zt;
     const int Zc = min(Zt, nz - z0);
     const int NO = N + 2 * H;                       // output rows
     const int O8 = (NO + OB - 1) / OB * OB;
@@ -168,11 +168,10 @@ __global__ void __launch_bounds__(512, 1)
     for (int i = threadIdx.x; i < SR * SC + TR * TS; i += blockDim.x) sm[i] = 0.f;
     const int grp = g.group[ga];
     const float *A = g.att ? g.A + (size_t)ga * g.Lp * g.nya * nz : nullptr;
-    const int x0 = item.y, x1 = item.z;
+    const int x0 = x0_, x1 = x1_;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
     const int cz_lo = max(0, H - z0), cz_hi = min(Z8 + 2 * H, nz - z0 + H);
     const int ncol = cz_hi - cz_lo;
-    const float *P = proj + (size_t)slot * N * nz;
     const bool att_inside = A && !g.att_first;  // "pa": A multiplies before the blur
     __syncthreads();
     if (!att_inside) {
@@ -184,7 +183,6 @@ __global__ void __launch_bounds__(512, 1)
     float th[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * ga + k];
-    int2 *wr = g.wrange + (size_t)slot * g.Lp;
     int parity = 0;
 #ifdef GB_PHASE_TIMING
     unsigned long long tacc[16] = {};
@@ -254,7 +252,7 @@ __global__ void __launch_bounds__(512, 1)
             t0 = t1;
         }
         {
-            float *Wp = W + ((size_t)slot * g.Lp + xp) * g.nya * nz;
+            float *Wp = Ws + (size_t)xp * g.nya * nz;
             const bool amul = Ap && g.att_first;
             // warp-tasks (32-row chunk, two z blocks of OP): lanes 0-15 and 16-31 take the
             // 16 row pairs of the chunk for z blocks 2q and 2q + 1
@@ -340,6 +338,38 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = 0; k < 16; k++) g_b1_phase_cycles[trow * 16 + k] = tacc[k];
     }
 #endif
+}
+
+// Grid (work item, z slab) over the angle slots of one group.
+template <int K, bool VEC, bool FIXED>
+__global__ void __launch_bounds__(512, 1)
+    k_b1_psf(SpectDev g, const float *__restrict__ proj, const int *__restrict__ alist,
+             const int4 *__restrict__ items, int Zt, float *__restrict__ W) {
+    const int4 item = items[blockIdx.x];  // (slot in group, first plane, end plane)
+    const int slot = item.x;
+    b1_psf_item<K, VEC, FIXED>(g, proj + (size_t)slot * g.N * g.nz, alist[slot],
+                               g.wrange + (size_t)slot * g.Lp, item.y, item.z, blockIdx.y * Zt,
+                               Zt, W + (size_t)slot * g.Lp * g.nya * g.nz);
+}
+
+// Persistent batch form of B1: one CTA per SM dequeues the group's work items of every
+// entry (N <= 128, nz <= 128: one fixed z slab), largest first.
+template <int K>
+__global__ void __launch_bounds__(512, 1) k_b1_psf_batch(const __grid_constant__ B1Batch p) {
+    __shared__ int s_item;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(p.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= p.n_items) return;
+        const int4 item = p.items[it];  // (slot in group, first plane, end plane, entry)
+        const int e = item.w, slot = item.x;
+        const SpectDev &g = p.g[e];
+        b1_psf_item<K, true, true>(g, p.proj[e] + (size_t)slot * g.N * g.nz, p.alist[e][slot],
+                                   g.wrange + (size_t)slot * g.Lp, item.y, item.z, 0, g.nz,
+                                   p.W[e] + (size_t)slot * g.Lp * g.nya * g.nz);
+    }
 }
 
 #ifdef GB_PHASE_TIMING
@@ -437,6 +467,33 @@ cudaError_t setup_b1(int K, size_t smem) {
         return setup_b1_k<KK>(smem);
         GB_FOR_EACH_K(GB_SETUP_CASE)
 #undef GB_SETUP_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t setup_b1_batch(int K) {
+    switch (K) {
+#define GB_SETUP_CASE(KK)                                                                  \
+    case KK:                                                                               \
+        return cudaFuncSetAttribute(k_b1_psf_batch<KK>,                                    \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,           \
+                                    (int)b1_psf_smem_bytes(KK, 128, 128));
+        GB_FOR_EACH_K(GB_SETUP_CASE)
+#undef GB_SETUP_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_b1_batch(int K, const B1Batch &p, int grid, cudaStream_t st) {
+    switch (K) {
+#define GB_LAUNCH_CASE(KK)                                                                 \
+    case KK:                                                                               \
+        k_b1_psf_batch<KK><<<grid, 512, b1_psf_smem_bytes(KK, 128, 128), st>>>(p);         \
+        return cudaGetLastError();
+        GB_FOR_EACH_K(GB_LAUNCH_CASE)
+#undef GB_LAUNCH_CASE
         default:
             return cudaErrorInvalidValue;
     }
@@ -694,16 +751,10 @@ __device__ __forceinline__ void apply_update4(int mode, const UpdateArgs &u, siz
 // Reference back-projector: for every object voxel, bilinear sample of W at the
 // back-rotation (angle 270 - beta) of each angle of the group, summed.  Threads own
 // (x, y, z quad); two angles are sampled before accumulating to keep loads in flight.
-template <bool PRIOR>
-__global__ void __launch_bounds__(256)
-    k_b2_gather4(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
-                 int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int x = blockIdx.z;
-    const int N = g.N, nz = g.nz;
-    if (4 * q >= nz || y >= N) return;
-    const int z = 4 * q;
+__device__ __forceinline__ float4 b2_gather_sum4(const SpectDev &g, const float *__restrict__ W,
+                                                  const int *__restrict__ alist, int n_slots,
+                                                  int x, int y, int z) {
+    const int nz = g.nz;
     const float lr = g.lin[x + g.pad], lc = g.lin[y + g.pad];
     const size_t slab = (size_t)g.Lp * g.nya * nz;
     float4 bp = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -735,8 +786,58 @@ __global__ void __launch_bounds__(256)
         bp.z = __fadd_rn(bp.z, v1.z);
         bp.w = __fadd_rn(bp.w, v1.w);
     }
+    return bp;
+}
+
+template <bool PRIOR>
+__global__ void __launch_bounds__(256)
+    k_b2_gather4(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
+                 int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = blockIdx.z;
+    const int N = g.N, nz = g.nz;
+    if (4 * q >= nz || y >= N) return;
+    const int z = 4 * q;
+    const float4 bp = b2_gather_sum4(g, W, alist, n_slots, x, y, z);
     const size_t i = ((size_t)x * N + y) * nz + z;
     apply_update4<PRIOR>(mode, u, i, x, y, z, N, N, nz, bp, out);
+}
+
+// Entry of a block of the batched gather / scatter kernels (the entries' blocks are
+// contiguous ranges of the grid, in entry order).
+__device__ __forceinline__ int batch_entry(const int *block_off, int b) {
+    int e = 0;
+    while (e + 1 < kMaxBatch && b >= block_off[e + 1]) e++;
+    return e;
+}
+
+int b2_gather_blocks(const SpectDev &g) {
+    return (int)(((long long)g.N * g.N * (g.nz / 4) + 255) / 256);
+}
+
+// Batched reference back-projector with its epilogue: a thread per (x, y, z quad) of an
+// entry's object (nz % 4 == 0), flat over the entry's voxels.
+__global__ void __launch_bounds__(256) k_b2_gather_batch(const __grid_constant__ B2Batch p) {
+    const int e = batch_entry(p.block_off, blockIdx.x);
+    const SpectDev &g = p.g[e];
+    const long long q = (long long)(blockIdx.x - p.block_off[e]) * 256 + threadIdx.x;
+    const int N = g.N, nz = g.nz, nq = nz / 4;
+    if (q >= (long long)N * N * nq) return;
+    const int z = 4 * (int)(q % nq), y = (int)((q / nq) % N), x = (int)(q / ((long long)nq * N));
+    const float4 bp = b2_gather_sum4(g, p.W[e], p.alist[e], p.n_slots[e], x, y, z);
+    const size_t i = ((size_t)x * N + y) * nz + z;
+    UpdateArgs u{};
+    u.f = p.out[e];
+    u.nbp = p.nbp[e];
+    u.acc = p.acc[e];
+    apply_update4<false>(p.mode[e], u, i, x, y, z, N, N, nz, bp, p.out[e]);
+}
+
+cudaError_t launch_b2_gather_batch(const B2Batch &p, int n_blocks, cudaStream_t st) {
+    if (n_blocks <= 0) return cudaSuccess;
+    k_b2_gather_batch<<<n_blocks, 256, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(256)
@@ -835,6 +936,49 @@ __global__ void __launch_bounds__(256)
         else
             atomicAdd(o, __fmul_rn(wt[q], v[0]));
     }
+}
+
+int b2_scatter_blocks(const SpectDev &g, int n_slots) {
+    return n_slots * g.Lp * ((g.nya * (g.nz / 4) + 255) / 256);
+}
+
+// Batched exact adjoint: the blocks of an entry cover (slot, plane, 256 (row, z quad) of
+// the plane), as k_b2_scatter's grid does; nz % 4 == 0 and 16-byte aligned objects.
+__global__ void __launch_bounds__(256) k_b2_scatter_batch(const __grid_constant__ B2Batch p) {
+    const int e = batch_entry(p.block_off, blockIdx.x);
+    const SpectDev &g = p.g[e];
+    const int per_plane = (g.nya * (g.nz / 4) + 255) / 256;
+    const int b = blockIdx.x - p.block_off[e];
+    const int slot = b / (per_plane * g.Lp), xp = (b / per_plane) % g.Lp;
+    const int i = (b % per_plane) * 256 + threadIdx.x;
+    const int nzv = g.nz / 4;
+    if (slot >= p.n_slots[e] || i >= g.nya * nzv) return;
+    const int r = i / nzv, z = (i % nzv) * 4;
+    const int2 rg = g.wrange[(size_t)slot * g.Lp + xp];
+    if (r < rg.x || r >= rg.y) return;
+    const float4 t = *reinterpret_cast<const float4 *>(
+        p.W[e] + (((size_t)slot * g.Lp + xp) * g.nya + r) * g.nz + z);
+    if (t.x == 0.f && t.y == 0.f && t.z == 0.f && t.w == 0.f) return;
+    float ix, iy;
+    rot_coords(g.theta_fwd + 6 * p.alist[e][slot], g.lin[xp], g.lin[g.ya_lo + r], g.half, ix, iy);
+    const Bilin bl = bilin(ix, iy);
+    const int N = g.N, nz = g.nz;
+    const int r0 = bl.r0 - g.pad, c0 = bl.c0 - g.pad;
+    const float wt[4] = {bl.nw, bl.ne, bl.sw, bl.se};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int rr = r0 + (q >> 1), cc = c0 + (q & 1);
+        if ((unsigned)rr >= (unsigned)N || (unsigned)cc >= (unsigned)N) continue;
+        atomicAdd(reinterpret_cast<float4 *>(p.out[e] + ((size_t)rr * N + cc) * nz + z),
+                  make_float4(__fmul_rn(wt[q], t.x), __fmul_rn(wt[q], t.y), __fmul_rn(wt[q], t.z),
+                              __fmul_rn(wt[q], t.w)));
+    }
+}
+
+cudaError_t launch_b2_scatter_batch(const B2Batch &p, int n_blocks, cudaStream_t st) {
+    if (n_blocks <= 0) return cudaSuccess;
+    k_b2_scatter_batch<<<n_blocks, 256, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_b2_scatter(const SpectDev &g, const float *W, const int *alist, int n_slots,

@@ -116,6 +116,34 @@ __global__ void k_reduce(const int *__restrict__ ioff, int NZ, const float *__re
     out[o] = gproj[gi] / (pr + kDelta);
 }
 
+// Batched reduction: one row (entry, slot) per grid row; the items of the row are added
+// in plane order (the order of row_items), so results do not depend on the work queue.
+__global__ void k_reduce_batch(const __grid_constant__ ReduceBatch p) {
+    const int2 row = p.rows[blockIdx.y];
+    const int e = row.x, slot = row.y;
+    const int NZ = p.NZ[e];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NZ) return;
+    float v = 0.f;
+    for (int c = p.row_off[blockIdx.y]; c < p.row_off[blockIdx.y + 1]; c++)
+        v += p.partials[(size_t)p.row_items[c] * p.nz_max + i];
+    const size_t o = (size_t)slot * NZ + i;
+    if (!p.ratio) {
+        p.out[e][o] = v;
+        return;
+    }
+    const size_t gi = (size_t)p.alist[e][slot] * NZ + i;
+    const float pr = p.sadd[e] ? v + p.sadd[e][gi] : v;
+    p.out[e][o] = p.gproj[e][gi] / (pr + kDelta);
+}
+
+cudaError_t launch_reduce_batch(const ReduceBatch &p, int n_rows, cudaStream_t st) {
+    if (n_rows <= 0) return cudaSuccess;
+    dim3 grid((p.nz_max + 255) / 256, n_rows);
+    k_reduce_batch<<<grid, 256, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------- launchers
 static bool fwd_fixed_host(int K, int N, int Zt, int tpb) {
     int OB = (K <= 31) ? 8 : 4;

@@ -83,11 +83,15 @@ __device__ __forceinline__ bool plane_hits(const SpectDev &g, const float *th, i
 // TPB: 512 threads (16 warps), or 768 threads (24 warps: more rows of the gather in flight
 // per SM; the taps are read from shared memory to fit the smaller register budget).  One
 // CTA per SM either way.
+// One work item: planes [x0_, x1_) of angle ga for the z slab starting at z0; the item's
+// partial ray sums go to out ([N][nz]).  Called once per CTA by k_fwd_psf and once per
+// dequeued item by the persistent batch kernel.  Returns true when this thread's bounded
+// wait gave up (the plan's error word is then set).
 template <int K, bool VEC, bool FIXED, int TPB>
-__global__ void __launch_bounds__(TPB, 1)
-    k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
-              const int4 *__restrict__ items, int Zt, float *__restrict__ partials,
-              const __grid_constant__ CUtensorMap tmA) {
+__device__ __forceinline__ bool fwd_psf_item(const SpectDev &g, const float *__restrict__ f,
+                                             const int ga, const int x0_, const int x1_,
+                                             const int z0, const int Zt, float *__restrict__ out,
+                                             const CUtensorMap *tmA, unsigned long long *bar) {
     constexpr int H = K / 2;
     constexpr int ZW = 128;
     constexpr bool TAPS_SMEM = TPB > 512;
@@ -99,11 +103,7 @@ __global__ void __launch_bounds__(TPB, 1)
     constexpr bool PAIR = !TAPS_SMEM;
     constexpr int NT = PAIR ? 16 / OB : (OB == 8 ? 3 : 6);
     using Acc = std::conditional_t<PAIR, float2, float>;
-    const int4 item = items[blockIdx.x];  // (slot, first plane, end plane)
-    const int slot = item.x;
-    const int ga = alist[slot];
     const int N = g.N, nz = g.nz;
-    const int z0 = blockIdx.y * Zt;
     const int Zc = min(Zt, nz - z0);
     const int N8 = (N + OB - 1) / OB * OB;
     const int Z8 = (Zc + OB - 1) / OB * OB;
@@ -115,8 +115,6 @@ __global__ void __launch_bounds__(TPB, 1)
     float *S = sm;
     float *Tt = S + SR * SC;
     float *tp = Tt + TR * TS;
-    unsigned long long *bar =
-        reinterpret_cast<unsigned long long *>(tp + ((4 * K + 1) & ~1));
     for (int i = threadIdx.x; i < SR * SC + TR * TS; i += TPB) sm[i] = 0.f;
 
     float th[6];
@@ -127,7 +125,7 @@ __global__ void __launch_bounds__(TPB, 1)
     const bool amul = A && g.att_first;
     const bool use_tma = VEC && amul;
     const bool tma_box = SC <= 256;  // 2-D boxes (else one 1-D copy per row)
-    const int x0 = item.y, x1 = item.z;
+    const int x0 = x0_, x1 = x1_;
     const int zv_lo = max(0, z0 - H), zv_hi = min(nz, z0 + Zc + H);  // z needed by the blur
     const int cz_lo = zv_lo - z0 + HP, cz_hi = zv_hi - z0 + HP;
     const int ncol = cz_hi - cz_lo;
@@ -211,7 +209,7 @@ __global__ void __launch_bounds__(TPB, 1)
             const int row0 = (ga * g.Lp + xp) * g.nya - g.ya_lo;  // tensor row of y = 0
             for (int k = lane; k < nbox; k += 32) {
                 const int ys = min(ra + k * kBoxRows, last);
-                tma_load_2d(S + (ys - (g.pad - H)) * SC, &tmA, z0 - HP, row0 + ys, bar);
+                tma_load_2d(S + (ys - (g.pad - H)) * SC, tmA, z0 - HP, row0 + ys, bar);
             }
         } else {
             const float *src = A + ((size_t)xp * g.nya + (ra - g.ya_lo)) * nz + zq_lo;
@@ -479,7 +477,6 @@ __global__ void __launch_bounds__(TPB, 1)
     }
 #endif
     // partial ray sums of this item
-    float *out = partials + (size_t)blockIdx.x * N * nz;
 #pragma unroll
     for (int k = 0; k < NT; k++) {
         const int y = ty[k], zb = tz[k];
@@ -496,6 +493,51 @@ __global__ void __launch_bounds__(TPB, 1)
                 }
             }
         }
+    }
+    return failed;
+}
+
+// One CTA per (work item, z slab) of one plan.
+template <int K, bool VEC, bool FIXED, int TPB>
+__global__ void __launch_bounds__(TPB, 1)
+    k_fwd_psf(SpectDev g, const float *__restrict__ f, const int *__restrict__ alist,
+              const int4 *__restrict__ items, int Zt, float *__restrict__ partials,
+              const __grid_constant__ CUtensorMap tmA) {
+    __shared__ unsigned long long bar;  // completion of the attenuation copies
+    const int4 item = items[blockIdx.x];  // (slot, first plane, end plane)
+    fwd_psf_item<K, VEC, FIXED, TPB>(g, f, alist[item.x], item.y, item.z, blockIdx.y * Zt, Zt,
+                                     partials + (size_t)blockIdx.x * g.N * g.nz, &tmA, &bar);
+}
+
+// Persistent batch form: one CTA per SM dequeues work items of several reconstructions
+// (or of several objects on one plan) from one list ordered by estimated cost, largest
+// first.  Every entry uses 512 threads, 16-byte z quads and the fixed 128 x 128 tile
+// (N <= 128, nz <= 128, one z slab).  The mbarrier is invalidated between items, when
+// none of its copies is in flight.
+template <int K>
+__global__ void __launch_bounds__(512, 1) k_fwd_psf_batch(const __grid_constant__ FwdBatch p) {
+    __shared__ unsigned long long bar;
+    __shared__ int s_item, s_failed;
+    if (threadIdx.x == 0) s_failed = 0;
+    bool used = false;
+    for (;;) {
+        __syncthreads();  // the previous item is finished by every thread
+        if (s_failed) return;  // a bounded wait gave up: stop dequeuing (error word is set)
+        if (threadIdx.x == 0) {
+            if (used) mbar_inval(&bar);
+            s_item = atomicAdd(p.counter, 1);
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= p.n_items) return;
+        const int4 item = p.items[it];  // (slot, first plane, end plane, entry)
+        const int e = item.w;
+        const SpectDev &g = p.g[e];
+        if (fwd_psf_item<K, true, true, 512>(g, p.f[e], p.alist[e][item.x], item.y, item.z, 0,
+                                             g.nz, p.partials + (size_t)it * p.nz_max, &p.tm[e],
+                                             &bar))
+            s_failed = 1;
+        used = g.att && g.att_first;
     }
 }
 
@@ -554,6 +596,15 @@ inline cudaError_t setup_fwd_t(size_t smem) {
 // Entry points of one tap bucket KK (one per spect_fwd_k*.cu translation unit, so the
 // buckets compile in parallel).
 #define GB_FWD_PSF_INSTANCE(KK)                                                              \
+    cudaError_t setup_fwd_psf_batch_##KK() {                                                 \
+        return cudaFuncSetAttribute(k_fwd_psf_batch<KK>,                                     \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,             \
+                                    (int)fwd_psf_smem_bytes(KK, 128, 128, 512));             \
+    }                                                                                        \
+    cudaError_t launch_fwd_psf_batch_##KK(const FwdBatch &p, int grid, cudaStream_t st) {    \
+        k_fwd_psf_batch<KK><<<grid, 512, fwd_psf_smem_bytes(KK, 128, 128, 512), st>>>(p);    \
+        return cudaGetLastError();                                                          \
+    }                                                                                        \
     cudaError_t launch_fwd_psf_##KK(const SpectDev &g, const float *f, const int *alist,     \
                                     const int4 *items, int n_items, int Zt, int tpb,         \
                                     float *partials, cudaStream_t st) {                     \

@@ -243,6 +243,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, u
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_inval(unsigned long long *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // Orders this thread's (and, after a CTA barrier, the CTA's) generic-proxy shared-memory
 // accesses before subsequent async-proxy (TMA) writes.
 __device__ __forceinline__ void fence_proxy_async_smem() {

@@ -121,6 +121,7 @@ struct gb_spect_plan {
     int Zt_fwd = 0, Zt_b1 = 0;
     int fwd_tpb = 512;  // forward CTA size: 512 or 768 threads (one CTA per SM)
     int fwd_items = 1, b1_items = 1;  // work items per resident CTA slot and z slab
+    unsigned lists_version = 0;       // bumped whenever the subset / work lists change
 };
 
 static void free_plan(gb_spect_plan *p) {
@@ -354,6 +355,7 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
     GB_CUDA(dev_alloc(&p->d_ioff, ioff.size() * sizeof(int)));
     GB_CUDA(cudaMemcpy(p->d_ioff, ioff.data(), ioff.size() * sizeof(int), cudaMemcpyHostToDevice));
     p->n_subsets = n_subsets;
+    p->lists_version++;
     size_t need = max_items * p->N * p->nz;
     if (need > p->partials_cap) {
         cudaFree(p->d_partials);
@@ -462,7 +464,7 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
             free_plan(p);
             return GB_ERR_ARG;
         }
-        K = psf_bucket(d->psf_k);
+        K = psf_bucket(std::max(d->psf_k, d->psf_k_min));
         if (K < 0) {
             set_error("PSF kernel of %d taps exceeds the compiled maximum (45)", d->psf_k);
             free_plan(p);
@@ -1050,3 +1052,468 @@ bool plan_forward_args(const gb_spect_plan *p, int subset, FwdArgs *a) {
 }
 
 }  // namespace gb
+
+// ======================================================================== batches
+// Several entries (reconstructions, or objects sharing one plan) projected by one persistent
+// launch per phase.  The work items of all entries are split by the plans' plane-cost
+// model into about kBatchWaves waves and ordered largest first, so small and large problems
+// fill the GPU together; partial sums are reduced per (entry, angle) in plane order.
+
+namespace gb {
+constexpr int kBatchWaves = 2;
+}
+
+struct gb_spect_batch {
+    int n = 0;
+    gb_spect_plan *plans[kMaxBatch] = {};
+    int K = 0, G = 16;
+    int n_lists = 0;  // 1 + n_subsets of the plans at creation
+    unsigned versions[kMaxBatch] = {};  // the plans' list versions at creation
+    int *d_alists = nullptr;            // every list's angles of every entry
+    int2 *wrange[kMaxBatch] = {};
+    float *W[kMaxBatch] = {};
+    float *ratio[kMaxBatch] = {};
+    float *bp[kMaxBatch] = {};
+    int slots_cap[kMaxBatch] = {};  // W slots of each entry
+    CUtensorMap tm[kMaxBatch];  // 64-byte aligned type
+    struct Lists {
+        int4 *fitems = nullptr;
+        int n_fitems = 0;
+        int2 *rows = nullptr;
+        int *row_off = nullptr, *row_items = nullptr;
+        int n_rows = 0;
+        std::vector<int4 *> bitems;  // per angle group
+        std::vector<int> n_bitems;
+        int n_groups = 0;
+        int n_sel[kMaxBatch] = {};
+        const int *alist[kMaxBatch] = {};  // device angle list of each entry
+    };
+    std::vector<Lists> lists;
+    float *partials = nullptr;
+    int nz_max = 0;
+    int *counters = nullptr;  // [2]: forward and B1 queues
+};
+
+static void free_batch(gb_spect_batch *b) {
+    if (!b) return;
+    for (int e = 0; e < kMaxBatch; e++) {
+        cudaFree(b->wrange[e]);
+        cudaFree(b->W[e]);
+        cudaFree(b->ratio[e]);
+        cudaFree(b->bp[e]);
+    }
+    for (auto &L : b->lists) {
+        cudaFree(L.fitems);
+        cudaFree(L.rows);
+        cudaFree(L.row_off);
+        cudaFree(L.row_items);
+        for (int4 *p : L.bitems) cudaFree(p);
+    }
+    cudaFree(b->partials);
+    cudaFree(b->counters);
+    cudaFree(b->d_alists);
+    delete b;
+}
+
+template <typename T>
+static gb_status upload_vec(T **dst, const std::vector<T> &v) {
+    GB_CUDA(dev_alloc(dst, std::max<size_t>(1, v.size()) * sizeof(T)));
+    if (!v.empty()) GB_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return GB_OK;
+}
+
+// Work items of the entries' angles (entry e: angles al[e][s0 .. s0 + n[e])), split by the
+// cost model into about kBatchWaves waves and sorted by cost, largest first; slot indices
+// are relative to s0.  order[k] = index of the k-th item in (entry, slot, plane) order.
+static void batch_items(const gb_spect_batch *b, const std::vector<std::vector<int>> &al,
+                        const std::vector<int> &s0, const std::vector<int> &n, bool fwd,
+                        std::vector<int4> &items, std::vector<int> &order) {
+    std::vector<std::vector<double>> w;
+    std::vector<int> ent, slot;
+    double total = 0;
+    for (int e = 0; e < b->n; e++)
+        for (int i = 0; i < n[e]; i++) {
+            w.push_back(plane_work(b->plans[e], al[e][s0[e] + i], fwd));
+            ent.push_back(e);
+            slot.push_back(i);
+            total += sum_of(w.back());
+        }
+    const int sms = b->plans[0]->sm_count;
+    const double target = total / std::max(1, kBatchWaves * sms);
+    std::vector<int4> raw;
+    std::vector<double> cost;
+    for (size_t k = 0; k < w.size(); k++) {
+        const int Lp = (int)w[k].size();
+        const int c = std::max(1, std::min(std::max(1, Lp / 4),
+                                           (int)std::lround(sum_of(w[k]) / std::max(target, 1.0))));
+        std::vector<int4> part;
+        split_planes(w[k], c, slot[k], part);
+        for (int4 it : part) {
+            it.w = ent[k];
+            double cst = 0;
+            for (int x = it.y; x < it.z; x++) cst += w[k][x];
+            raw.push_back(it);
+            cost.push_back(cst);
+        }
+    }
+    std::vector<int> idx(raw.size());
+    for (size_t k = 0; k < idx.size(); k++) idx[k] = (int)k;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+    items.resize(raw.size());
+    order.assign(raw.size(), 0);
+    for (size_t k = 0; k < idx.size(); k++) {
+        items[k] = raw[idx[k]];
+        order[idx[k]] = (int)k;
+    }
+}
+
+static bool batch_list_ok(const gb_spect_batch *b) {
+    for (int e = 0; e < b->n; e++)
+        if (b->plans[e]->lists_version != b->versions[e]) return false;
+    return true;
+}
+
+// SpectDev of entry e with its own W row ranges
+static SpectDev batch_dev(const gb_spect_batch *b, int e) {
+    SpectDev g = b->plans[e]->dev;
+    g.wrange = b->wrange[e];
+    return g;
+}
+
+static gb_status batch_forward(gb_spect_batch *b, int li, const float *const *objects, int ratio,
+                               float *const *out, const float *const *gproj,
+                               const float *const *sadd, cudaStream_t st) {
+    const gb_spect_batch::Lists &L = b->lists[li];
+    FwdBatch fp;
+    std::memset(&fp, 0, sizeof(fp));
+    for (int e = 0; e < b->n; e++) {
+        fp.tm[e] = b->tm[e];
+        fp.g[e] = batch_dev(b, e);
+        fp.f[e] = objects[e];
+        fp.alist[e] = L.alist[e];
+    }
+    fp.items = L.fitems;
+    fp.n_items = L.n_fitems;
+    fp.counter = b->counters;
+    fp.partials = b->partials;
+    fp.nz_max = b->nz_max;
+    GB_CUDA(cudaMemsetAsync(b->counters, 0, sizeof(int), st));
+    const int grid = std::max(1, std::min(L.n_fitems, b->plans[0]->sm_count));
+    cudaError_t err = cudaErrorInvalidValue;
+    switch (b->K) {
+#define GB_BATCH_CASE(KK)                                  \
+    case KK:                                               \
+        err = launch_fwd_psf_batch_##KK(fp, grid, st);     \
+        break;
+        GB_FOR_EACH_K(GB_BATCH_CASE)
+#undef GB_BATCH_CASE
+    }
+    GB_CUDA(err);
+    ReduceBatch rp;
+    std::memset(&rp, 0, sizeof(rp));
+    for (int e = 0; e < b->n; e++) {
+        rp.out[e] = out[e];
+        rp.gproj[e] = gproj ? gproj[e] : nullptr;
+        rp.sadd[e] = sadd ? sadd[e] : nullptr;
+        rp.alist[e] = L.alist[e];
+        rp.NZ[e] = b->plans[e]->N * b->plans[e]->nz;
+    }
+    rp.rows = L.rows;
+    rp.row_off = L.row_off;
+    rp.row_items = L.row_items;
+    rp.partials = b->partials;
+    rp.nz_max = b->nz_max;
+    rp.ratio = ratio;
+    GB_CUDA(launch_reduce_batch(rp, L.n_rows, st));
+    return GB_OK;
+}
+
+// Back projection of proj[e] (rows = the list's angles) in groups of G angles.
+// kind 0: reference operator into out[e]; 1: exact adjoint into out[e];
+// 2: fused OSEM update of out[e] (the objects) with norm_bp[e].
+static gb_status batch_backward(gb_spect_batch *b, int li, const float *const *proj, int kind,
+                                float *const *out, const float *const *norm_bp, cudaStream_t st) {
+    const gb_spect_batch::Lists &L = b->lists[li];
+    if (kind == 1)
+        for (int e = 0; e < b->n; e++) {
+            const gb_spect_plan *p = b->plans[e];
+            GB_CUDA(cudaMemsetAsync(out[e], 0, (size_t)p->N * p->N * p->nz * sizeof(float), st));
+        }
+    for (int gi = 0; gi < L.n_groups; gi++) {
+        B1Batch bp1;
+        std::memset(&bp1, 0, sizeof(bp1));
+        B2Batch bp2;
+        std::memset(&bp2, 0, sizeof(bp2));
+        int blocks = 0;
+        for (int e = 0; e < b->n; e++) {
+            const gb_spect_plan *p = b->plans[e];
+            const int a0 = gi * b->G, na = std::max(0, std::min(b->G, L.n_sel[e] - a0));
+            bp1.g[e] = bp2.g[e] = batch_dev(b, e);
+            bp1.proj[e] = proj[e] + (size_t)a0 * p->N * p->nz;
+            bp1.alist[e] = bp2.alist[e] = L.alist[e] + a0;
+            bp1.W[e] = b->W[e];
+            bp2.W[e] = b->W[e];
+            bp2.n_slots[e] = na;
+            bp2.block_off[e] = blocks;
+            const bool last = na > 0 && a0 + na == L.n_sel[e];
+            if (kind == 2) {
+                bp2.out[e] = last ? out[e] : b->bp[e];
+                bp2.nbp[e] = norm_bp[e];
+                bp2.acc[e] = (last && gi > 0) ? b->bp[e] : nullptr;
+                bp2.mode[e] = last ? B2_OSEM : (gi == 0 ? B2_WRITE : B2_ADD);
+            } else {
+                bp2.out[e] = out[e];
+                bp2.mode[e] = gi == 0 ? B2_WRITE : B2_ADD;
+            }
+            if (na > 0)
+                blocks += kind == 1 ? b2_scatter_blocks(bp2.g[e], na) : b2_gather_blocks(bp2.g[e]);
+        }
+        for (int e = b->n; e <= kMaxBatch; e++) bp2.block_off[e] = blocks;
+        bp1.items = L.bitems[gi];
+        bp1.n_items = L.n_bitems[gi];
+        bp1.counter = b->counters + 1;
+        GB_CUDA(cudaMemsetAsync(b->counters + 1, 0, sizeof(int), st));
+        if (L.n_bitems[gi] > 0)
+            GB_CUDA(launch_b1_batch(b->K, bp1, std::min(L.n_bitems[gi], b->plans[0]->sm_count),
+                                    st));
+        if (kind == 1)
+            GB_CUDA(launch_b2_scatter_batch(bp2, blocks, st));
+        else
+            GB_CUDA(launch_b2_gather_batch(bp2, blocks, st));
+    }
+    return GB_OK;
+}
+
+extern "C" {
+
+gb_status gb_spect_batch_create(gb_spect_plan *const *plans, int32_t n, gb_spect_batch **out) {
+    clear_error();
+    GB_CHECK_ARG(plans && out, "null argument");
+    *out = nullptr;
+    GB_CHECK_ARG(n >= 1 && n <= kMaxBatch, "a batch holds 1 to %d entries (got %d)", kMaxBatch, n);
+    auto *b = new gb_spect_batch();
+    b->n = n;
+    for (int e = 0; e < n; e++) {
+        gb_spect_plan *p = plans[e];
+        if (!p) {
+            free_batch(b);
+            set_error("null plan %d", e);
+            return GB_ERR_ARG;
+        }
+        const char *why = nullptr;
+        if (!p->dev.psf) why = "has no PSF";
+        else if (p->N > 128 || p->nz > 128) why = "is larger than 128 x 128 x 128";
+        else if (p->nz % 4 != 0) why = "has nz not divisible by 4";
+        else if (e > 0 && p->dev.K != b->plans[0]->dev.K) why = "has another PSF tap bucket";
+        else if (e > 0 && p->lists.size() != b->plans[0]->lists.size()) why = "has another subset count";
+        if (why) {
+            set_error("plan %d %s: batches need PSF plans of one tap bucket (psf_k_min), one "
+                      "subset count, N and nz <= 128 and nz %% 4 == 0", e, why);
+            free_batch(b);
+            return GB_ERR_UNSUPPORTED;
+        }
+        b->plans[e] = p;
+    }
+    b->K = b->plans[0]->dev.K;
+    if (fwd_psf_smem_bytes(b->K, 128, 128, 512) > max_smem_optin() ||
+        b1_psf_smem_bytes(b->K, 128, 128) > max_smem_optin()) {
+        set_error("the %d-tap batch tiles do not fit shared memory", b->K);
+        free_batch(b);
+        return GB_ERR_UNSUPPORTED;
+    }
+    b->n_lists = (int)b->plans[0]->lists.size();
+#define BFAIL(st_)                   \
+    do {                             \
+        gb_status s_ = (st_);        \
+        if (s_ != GB_OK) {           \
+            free_batch(b);           \
+            return s_;               \
+        }                            \
+    } while (0)
+#define BCUDA(call)                                                                      \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            set_error("%s failed: %s", #call, cudaGetErrorString(e_));                   \
+            free_batch(b);                                                               \
+            return e_ == cudaErrorMemoryAllocation ? GB_ERR_OOM : GB_ERR_CUDA;           \
+        }                                                                                \
+    } while (0)
+    switch (b->K) {
+#define GB_SETUP_CASE(KK)                       \
+    case KK:                                    \
+        BCUDA(setup_fwd_psf_batch_##KK());      \
+        break;
+        GB_FOR_EACH_K(GB_SETUP_CASE)
+#undef GB_SETUP_CASE
+    }
+    BCUDA(setup_b1_batch(b->K));
+    size_t max_items = 1;
+    for (int e = 0; e < n; e++) b->nz_max = std::max(b->nz_max, b->plans[e]->N * b->plans[e]->nz);
+    b->lists.resize(b->n_lists);
+    std::vector<int> all_angles;
+    std::vector<std::vector<size_t>> alist_off(b->n_lists, std::vector<size_t>(n));
+    for (int e = 0; e < n; e++) b->versions[e] = b->plans[e]->lists_version;
+    for (int li = 0; li < b->n_lists; li++) {
+        gb_spect_batch::Lists &L = b->lists[li];
+        std::vector<std::vector<int>> al(n);
+        std::vector<int> s0(n, 0), cnt(n);
+        for (int e = 0; e < n; e++) {
+            const gb_spect_plan *p = b->plans[e];
+            const gb_spect_plan::List &pl = p->lists[li];
+            std::vector<int> h(pl.n);
+            BCUDA(cudaMemcpy(h.data(), p->d_alist + pl.alist_off, pl.n * sizeof(int),
+                             cudaMemcpyDeviceToHost));
+            al[e] = h;
+            cnt[e] = pl.n;
+            L.n_sel[e] = pl.n;
+            alist_off[li][e] = all_angles.size();
+            all_angles.insert(all_angles.end(), h.begin(), h.end());
+            b->slots_cap[e] = std::max(b->slots_cap[e], std::min(b->G, pl.n));
+            L.n_groups = std::max(L.n_groups, (pl.n + b->G - 1) / b->G);
+        }
+        // forward items and the reduction rows
+        std::vector<int4> fit;
+        std::vector<int> order;
+        batch_items(b, al, s0, cnt, true, fit, order);
+        std::vector<int2> rows;
+        std::vector<int> row_off{0}, row_items;
+        {
+            // the unsorted items come in (entry, slot, plane) order: group them by row
+            std::vector<int4> raw(fit.size());
+            for (size_t k = 0; k < order.size(); k++) raw[k] = fit[order[k]];
+            size_t k = 0;
+            for (int e = 0; e < n; e++)
+                for (int s = 0; s < cnt[e]; s++) {
+                    rows.push_back(make_int2(e, s));
+                    while (k < raw.size() && raw[k].w == e && raw[k].x == s)
+                        row_items.push_back(order[k++]);
+                    row_off.push_back((int)row_items.size());
+                }
+        }
+        L.n_fitems = (int)fit.size();
+        L.n_rows = (int)rows.size();
+        max_items = std::max(max_items, fit.size());
+        BFAIL(upload_vec(&L.fitems, fit));
+        BFAIL(upload_vec(&L.rows, rows));
+        BFAIL(upload_vec(&L.row_off, row_off));
+        BFAIL(upload_vec(&L.row_items, row_items));
+        // B1 items per angle group
+        for (int gi = 0; gi < L.n_groups; gi++) {
+            std::vector<int> gs0(n), gcnt(n);
+            for (int e = 0; e < n; e++) {
+                gs0[e] = gi * b->G;
+                gcnt[e] = std::max(0, std::min(b->G, cnt[e] - gs0[e]));
+            }
+            std::vector<int4> bit;
+            std::vector<int> border;
+            batch_items(b, al, gs0, gcnt, false, bit, border);
+            int4 *d = nullptr;
+            gb_status st = upload_vec(&d, bit);
+            L.bitems.push_back(d);
+            L.n_bitems.push_back((int)bit.size());
+            BFAIL(st);
+        }
+    }
+    BFAIL(upload_vec(&b->d_alists, all_angles));
+    for (int li = 0; li < b->n_lists; li++)
+        for (int e = 0; e < n; e++) b->lists[li].alist[e] = b->d_alists + alist_off[li][e];
+    for (int e = 0; e < n; e++) {
+        const gb_spect_plan *p = b->plans[e];
+        const size_t slab = (size_t)p->Lp * p->dev.nya * p->nz;
+        BCUDA(dev_alloc(&b->W[e], (size_t)b->slots_cap[e] * slab * sizeof(float)));
+        BCUDA(dev_alloc(&b->wrange[e], (size_t)b->slots_cap[e] * p->Lp * sizeof(int2)));
+        BCUDA(cudaMemset(b->wrange[e], 0, (size_t)b->slots_cap[e] * p->Lp * sizeof(int2)));
+        size_t max_sel = 1;
+        bool multi = false;
+        for (const auto &L : b->lists) {
+            max_sel = std::max(max_sel, (size_t)L.n_sel[e]);
+            multi = multi || L.n_sel[e] > b->G;
+        }
+        BCUDA(dev_alloc(&b->ratio[e], max_sel * p->N * p->nz * sizeof(float)));
+        if (multi) BCUDA(dev_alloc(&b->bp[e], (size_t)p->N * p->N * p->nz * sizeof(float)));
+        const int HP = (b->K / 2 + 3) / 4 * 4;
+        BCUDA(make_att_tmap(p->dev, fwd_s_cols(128, HP), &b->tm[e]));
+    }
+    BCUDA(dev_alloc(&b->partials, max_items * b->nz_max * sizeof(float)));
+    BCUDA(dev_alloc(&b->counters, 2 * sizeof(int)));
+#undef BFAIL
+#undef BCUDA
+    *out = b;
+    return GB_OK;
+}
+
+gb_status gb_spect_batch_destroy(gb_spect_batch *b) {
+    clear_error();
+    if (b) {
+        cudaDeviceSynchronize();
+        free_batch(b);
+    }
+    return GB_OK;
+}
+
+static gb_status batch_list(const gb_spect_batch *b, int subset, int *li) {
+    if (!batch_list_ok(b)) {
+        set_error("a plan's subsets or tiles changed after the batch was created; create it "
+                  "again");
+        return GB_ERR_STATE;
+    }
+    *li = subset < 0 ? 0 : subset + 1;
+    if (*li >= b->n_lists) {
+        set_error("subset %d out of range (n_subsets=%d)", subset, b->n_lists - 1);
+        return GB_ERR_STATE;
+    }
+    return GB_OK;
+}
+
+gb_status gb_spect_batch_forward(gb_spect_batch *b, const float *const *objects,
+                                 float *const *proj, int32_t subset, gb_stream_t stream) {
+    clear_error();
+    GB_INJECT_ARG();
+    GB_CHECK_ARG(b && objects && proj, "null argument");
+    for (int e = 0; e < b->n; e++) GB_CHECK_ARG(objects[e] && proj[e], "null buffer of entry %d", e);
+    GB_INJECT_LAUNCH();
+    int li;
+    gb_status s = batch_list(b, subset, &li);
+    if (s != GB_OK) return s;
+    return batch_forward(b, li, objects, 0, proj, nullptr, nullptr, as_stream(stream));
+}
+
+gb_status gb_spect_batch_backward(gb_spect_batch *b, const float *const *proj,
+                                  float *const *objects, int32_t subset, int32_t adjoint,
+                                  gb_stream_t stream) {
+    clear_error();
+    GB_INJECT_ARG();
+    GB_CHECK_ARG(b && proj && objects, "null argument");
+    for (int e = 0; e < b->n; e++) {
+        GB_CHECK_ARG(proj[e] && objects[e], "null buffer of entry %d", e);
+        GB_CHECK_ARG(!adjoint || ((uintptr_t)objects[e] & 15) == 0,
+                     "object %d must be 16-byte aligned (vector atomics)", e);
+    }
+    GB_INJECT_LAUNCH();
+    int li;
+    gb_status s = batch_list(b, subset, &li);
+    if (s != GB_OK) return s;
+    return batch_backward(b, li, proj, adjoint ? 1 : 0, objects, nullptr, as_stream(stream));
+}
+
+gb_status gb_spect_batch_osem_step(gb_spect_batch *b, float *const *objects,
+                                   const float *const *projections, const float *const *additive,
+                                   const float *const *norm_bp, int32_t subset,
+                                   gb_stream_t stream) {
+    clear_error();
+    GB_INJECT_ARG();
+    GB_CHECK_ARG(b && objects && projections && norm_bp, "null argument");
+    for (int e = 0; e < b->n; e++)
+        GB_CHECK_ARG(objects[e] && projections[e] && norm_bp[e], "null buffer of entry %d", e);
+    GB_INJECT_LAUNCH();
+    int li;
+    gb_status s = batch_list(b, subset, &li);
+    if (s != GB_OK) return s;
+    cudaStream_t st = as_stream(stream);
+    s = batch_forward(b, li, objects, 1, b->ratio, projections, additive, st);
+    if (s != GB_OK) return s;
+    return batch_backward(b, li, b->ratio, 2, objects, norm_bp, st);
+}
+
+}  // extern "C"

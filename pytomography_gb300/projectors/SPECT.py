@@ -19,6 +19,11 @@ from ..transforms.SPECT import SPECTAttenuationTransform, SPECTPSFTransform
 from .system_matrix import SystemMatrix
 
 
+# PSF tap counts the fused kernels are compiled for (a plan's taps are zero-padded to the
+# smallest that holds them)
+PSF_BUCKETS = (7, 11, 15, 21, 25, 29, 37, 45)
+
+
 class SPECTSystemMatrix(SystemMatrix):
     """Rotate+sum SPECT system matrix.
 
@@ -43,7 +48,8 @@ class SPECTSystemMatrix(SystemMatrix):
     def __init__(self, obj2obj_transforms, proj2proj_transforms, object_meta, proj_meta,
                  object_initial_based_on_camera_path: bool = False,
                  psf_trunc_rel: float = 1e-7, autotune: bool = False,
-                 check_device_status: bool = False, _no_pad: bool = False) -> None:
+                 check_device_status: bool = False, _no_pad: bool = False,
+                 _psf_k_min: int = 0) -> None:
         if proj2proj_transforms:
             raise NotImplementedError("proj2proj transforms are not part of the fused path")
         super().__init__(object_meta, proj_meta, obj2obj_transforms, proj2proj_transforms)
@@ -52,6 +58,8 @@ class SPECTSystemMatrix(SystemMatrix):
         self.autotune_enabled = bool(autotune)
         self.check_device_status = bool(check_device_status)
         self._no_pad = bool(_no_pad)  # unpadded rotation frame (the StarGuide projector)
+        self._psf_k_min = int(_psf_k_min)  # smallest PSF tap bucket (plans batched together)
+        self._lists_epoch = 0  # bumped whenever the plan's subset or tile lists change
         self._plan = None
         self._lib = _lib.load()
         self._build_plan()
@@ -146,6 +154,7 @@ class SPECTSystemMatrix(SystemMatrix):
         else:
             self._psf_k = 1
         desc.no_pad = 1 if self._no_pad else 0
+        desc.psf_k_min = self._psf_k_min
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             torch.cuda.synchronize()
@@ -177,6 +186,26 @@ class SPECTSystemMatrix(SystemMatrix):
                                "for its attenuation copies; outputs since the last check are "
                                "invalid")
 
+    @property
+    def psf_bucket(self) -> int:
+        """Tap count the plan's PSF kernels are compiled for (0 without PSF)."""
+        if "p" not in self._order:
+            return 0
+        k = max(self._psf_k, self._psf_k_min)
+        return next(b for b in PSF_BUCKETS if k <= b)
+
+    def _rebuild_plan(self, psf_k_min: int) -> None:
+        """Create the plan again with at least ``psf_k_min`` taps per PSF kernel (the same
+        projections: the extra taps are zero), keeping the current subsets."""
+        old = self._plan
+        self._psf_k_min = int(psf_k_min)
+        self._build_plan()
+        if old is not None:
+            self._lib.gb_spect_plan_destroy(old)
+        if self.subset_indices_array is not None and self.n_subsets > 1:
+            _lib.check(self._lib.gb_spect_set_subsets(self._plan, int(self.n_subsets)))
+        self._lists_epoch += 1
+
     def _after_call(self) -> None:
         if self.check_device_status:
             self.raise_on_device_error()
@@ -187,6 +216,7 @@ class SPECTSystemMatrix(SystemMatrix):
         self.subset_indices_array = [indices[i::n_subsets] for i in range(n_subsets)]
         self.n_subsets = n_subsets
         _lib.check(self._lib.gb_spect_set_subsets(self._plan, int(n_subsets)))
+        self._lists_epoch += 1
         if self.autotune_enabled:
             self.autotune()
 
@@ -194,7 +224,7 @@ class SPECTSystemMatrix(SystemMatrix):
     def _tuning_key(self, subset_idx):
         props = torch.cuda.get_device_properties(self.device)
         return (props.name, tuple(int(v) for v in self.object_meta.shape),
-                tuple(float(v) for v in self.object_meta.dr), self._order, self._psf_k,
+                tuple(float(v) for v in self.object_meta.dr), self._order, self.psf_bucket,
                 int(self.proj_meta.num_projections), int(self.n_subsets),
                 self._n_sel(subset_idx))
 
@@ -206,6 +236,7 @@ class SPECTSystemMatrix(SystemMatrix):
     def set_tuning(self, **fields) -> None:
         t = _lib.SpectTuning(**{**self.get_tuning(), **fields})
         _lib.check(self._lib.gb_spect_set_tuning(self._plan, ctypes.byref(t)))
+        self._lists_epoch += 1
 
     def autotune(self, subset_idx: int | None = 0, reps: int = 3) -> dict:
         """Pick the fastest kernel tiles for this geometry (gb_spect_autotune), timing
@@ -219,6 +250,7 @@ class SPECTSystemMatrix(SystemMatrix):
             self.set_tuning(**hit)
             return dict(hit)
         out = _lib.SpectTuning()
+        self._lists_epoch += 1
         with torch.cuda.device(self.device):
             torch.cuda.synchronize()
             _lib.check(self._lib.gb_spect_autotune(
