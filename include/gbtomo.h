@@ -308,6 +308,14 @@ gb_status gb_pet_forward(gb_pet_plan *plan, const float *img, float *proj, int32
  * img must be 16-byte aligned (vector atomics). */
 gb_status gb_pet_backward(gb_pet_plan *plan, const float *proj, float *img, int32_t subset,
                           gb_stream_t stream);
+/* Deterministic back projection for reproducibility (no counterpart in the reference):
+ * with on = 1, gb_pet_backward accumulates every contribution as a 64-bit fixed-point
+ * integer (scale 2^k with k chosen on the device from the largest |proj| of the call so
+ * that no sum can overflow) and converts the sums to float at the end; the results are
+ * then bit-identical from run to run, whatever the order of the atomic additions, and
+ * agree with the float path to rounding.  Allocates an int64 image (call at set-up);
+ * on = 0 frees it and restores the float-atomic path. */
+gb_status gb_pet_set_deterministic(gb_pet_plan *plan, int32_t on);
 /* Non-TOF line integrals of `img` along the subset's events (attenuation path,
  * petlm_system_matrix.py:91-110); use_tof selects the TOF kernel instead. */
 gb_status gb_pet_lor_forward(gb_pet_plan *plan, const float *img, float *proj, int32_t subset,

@@ -121,6 +121,7 @@ SIGNATURES = [
     ("gb_pet_set_subsets", c_int, [c_void_p, c_int]),
     ("gb_pet_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     ("gb_pet_backward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    ("gb_pet_set_deterministic", c_int, [c_void_p, c_int]),
     ("gb_pet_lor_forward", c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]),
     ("gb_pet_sensitivity", c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p, c_void_p,
                                    c_float, c_void_p, c_void_p]),

@@ -59,6 +59,51 @@ __global__ void __launch_bounds__(256)
     joseph<true, TOF>(g, p0, p1, img, nullptr, r.z, v);
 }
 
+// Deterministic back projection: the same traces accumulated as 64-bit fixed-point sums.
+template <bool TOF>
+__global__ void __launch_bounds__(256)
+    k_pet_bwd_det(PetDev g, const int4 *__restrict__ rec, long long n,
+                  const float *__restrict__ proj, const float *__restrict__ scale,
+                  unsigned long long *__restrict__ acc) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int4 r = rec[k];
+    const float v = proj[(long long)r.w];
+    if (v == 0.f) return;
+    const float *p0 = g.lut + 3 * (long long)r.x;
+    const float *p1 = g.lut + 3 * (long long)r.y;
+    joseph<true, TOF, true>(g, p0, p1, reinterpret_cast<float *>(acc), nullptr, r.z, v, *scale);
+}
+
+// Largest |proj| of the list (atomicMax on the bit patterns of non-negative floats, which
+// order like the values; the result does not depend on the order).
+__global__ void k_abs_max(const int4 *__restrict__ rec, long long n, const float *__restrict__ proj,
+                          unsigned *__restrict__ out) {
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    float m = 0.f;
+    if (k < n) m = fabsf(proj[(long long)rec[k].w]);
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
+}
+
+// Fixed-point scale: a power of two such that n events of magnitude <= max|proj|, each
+// adding at most cf_max (the longest plane step) to a voxel, stay below 2^61.
+__global__ void k_det_scale(const unsigned *__restrict__ maxbits, long long n, float cf_max,
+                            float *__restrict__ scale) {
+    const double bound = (double)__uint_as_float(*maxbits) * (double)n * (double)cf_max;
+    int e = 0;
+    if (bound > 0.0) frexp(bound, &e);  // bound < 2^e
+    *scale = (float)ldexp(1.0, max(-100, min(100, 61 - e)));
+}
+
+__global__ void k_det_to_float(const unsigned long long *__restrict__ acc,
+                               const float *__restrict__ scale, float *__restrict__ img,
+                               long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    img[i] = (float)((double)(long long)acc[i] / (double)*scale);
+}
+
 // Locality key of list event j: principal axis (2 bits), transaxial direction in 8 bins
 // over [0, pi) (3 bits) and the Morton code of the TOF-window centre (the LOR midpoint
 // without TOF) in cells of 8 voxels, 6 bits per axis (18 bits).
@@ -173,6 +218,11 @@ struct gb_pet_plan {
     int4 *d_rec = nullptr;
     float *d_tof_tab = nullptr;
     std::vector<long long> list_off;
+    // deterministic back projection: fixed-point sums [img_size], the list's max |proj|
+    // bits and the fixed-point scale
+    unsigned long long *d_acc64 = nullptr;
+    unsigned *d_maxbits = nullptr;
+    float *d_scale = nullptr;
 };
 
 static void pet_free(gb_pet_plan *p) {
@@ -183,6 +233,9 @@ static void pet_free(gb_pet_plan *p) {
     cudaFree(p->d_bp);
     cudaFree(p->d_rec);
     cudaFree(p->d_tof_tab);
+    cudaFree(p->d_acc64);
+    cudaFree(p->d_maxbits);
+    cudaFree(p->d_scale);
     delete p;
 }
 
@@ -400,11 +453,42 @@ gb_status gb_pet_backward(gb_pet_plan *p, const float *proj, float *img, int32_t
     if (n == 0) return GB_OK;
     unsigned blocks = (unsigned)((n + 255) / 256);
     const int4 *rec = list_tiles(p, subset);
+    if (p->d_acc64) {  // deterministic mode
+        const float cf_max = 1.7320509f * std::max(p->dev.vox[0], std::max(p->dev.vox[1], p->dev.vox[2]));
+        GB_CUDA(cudaMemsetAsync(p->d_maxbits, 0, sizeof(unsigned), st));
+        k_abs_max<<<blocks, 256, 0, st>>>(rec, n, proj, p->d_maxbits);
+        k_det_scale<<<1, 1, 0, st>>>(p->d_maxbits, n, cf_max, p->d_scale);
+        GB_CUDA(cudaMemsetAsync(p->d_acc64, 0, (size_t)p->img_size * sizeof(unsigned long long), st));
+        if (p->dev.tof)
+            k_pet_bwd_det<true><<<blocks, 256, 0, st>>>(p->dev, rec, n, proj, p->d_scale, p->d_acc64);
+        else
+            k_pet_bwd_det<false><<<blocks, 256, 0, st>>>(p->dev, rec, n, proj, p->d_scale, p->d_acc64);
+        k_det_to_float<<<(unsigned)((p->img_size + 255) / 256), 256, 0, st>>>(
+            p->d_acc64, p->d_scale, img, p->img_size);
+        GB_LAUNCH_CHECK();
+        return GB_OK;
+    }
     if (p->dev.tof)
         k_pet_bwd<true><<<blocks, 256, 0, st>>>(p->dev, rec, n, proj, 0, img);
     else
         k_pet_bwd<false><<<blocks, 256, 0, st>>>(p->dev, rec, n, proj, 0, img);
     GB_LAUNCH_CHECK();
+    return GB_OK;
+}
+
+gb_status gb_pet_set_deterministic(gb_pet_plan *p, int32_t on) {
+    clear_error();
+    GB_CHECK_ARG(p, "null plan");
+    cudaFree(p->d_acc64);
+    cudaFree(p->d_maxbits);
+    cudaFree(p->d_scale);
+    p->d_acc64 = nullptr;
+    p->d_maxbits = nullptr;
+    p->d_scale = nullptr;
+    if (!on) return GB_OK;
+    GB_CUDA(dev_alloc(&p->d_acc64, (size_t)p->img_size * sizeof(unsigned long long)));
+    GB_CUDA(dev_alloc(&p->d_maxbits, sizeof(unsigned)));
+    GB_CUDA(dev_alloc(&p->d_scale, sizeof(float)));
     return GB_OK;
 }
 

@@ -63,10 +63,21 @@ __device__ __forceinline__ int pick(int a, int b, int c, int k) {
 // other axes (in voxel units) and the TOF distance s are linear in the plane index i and
 // are evaluated as base + i * step.  Axis-dependent quantities are selected into
 // registers once (no dynamically indexed local arrays).
-template <bool BACK, bool TOF>
+// DET (back projection only): img is an array of 64-bit integers holding fixed-point sums
+// with `scale` units per 1.0; each contribution is rounded to that grid and added with an
+// integer atomic, so the sums do not depend on the order of the additions.
+template <bool BACK, bool TOF, bool DET = false>
 __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict__ p0,
                                         const float *__restrict__ p1, float *img,
-                                        const float *__restrict__ cimg, int tbin, float val) {
+                                        const float *__restrict__ cimg, int tbin, float val,
+                                        float scale = 0.f) {
+    auto add = [&](int off, float v) {
+        if constexpr (DET)
+            atomicAdd(reinterpret_cast<unsigned long long *>(img) + off,
+                      (unsigned long long)__float2ll_rn(v * scale));
+        else
+            atomicAdd(img + off, v);
+    };
     const float ax = p0[0], ay = p0[1], az = p0[2];
     const float dx = p1[0] - ax, dy = p1[1] - ay, dz = p1[2] - az;
     const float len = sqrtf(dx * dx + dy * dy + dz * dz);
@@ -198,7 +209,7 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
                 const float v0 = wr * (1.f - wz), v1 = wr * wz;
                 const int off = base + r * so + jz;
                 const int qd = off & 3;  // the pair's position in its aligned quad
-                if (ok0 && ok1 && qd < 3 && off - qd + 4 <= g.n_vox) {
+                if (!DET && ok0 && ok1 && qd < 3 && off - qd + 4 <= g.n_vox) {
                     // both corners in one 16-byte quad: one vector atomic (zeros elsewhere)
                     float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (qd == 0) {
@@ -213,8 +224,8 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
                     }
                     atomicAdd(reinterpret_cast<float4 *>(img + (off - qd)), v4);
                 } else {
-                    if (ok0) atomicAdd(img + off, v0);
-                    if (ok1) atomicAdd(img + off + 1, v1);
+                    if (ok0) add(off, v0);
+                    if (ok1) add(off + 1, v1);
                 }
             }
             continue;
@@ -226,7 +237,7 @@ __device__ __forceinline__ float joseph(const PetDev &g, const float *__restrict
             const float wq = ((q & 1) ? wa : 1.f - wa) * ((q >> 1) ? wb : 1.f - wb);
             const int off = base + ja * sa + jb * sb;
             if (BACK)
-                atomicAdd(img + off, val * w * wq);
+                add(off, val * w * wq);
             else
                 acc += w * wq * __ldg(cimg + off);
         }

@@ -72,11 +72,13 @@ int device_sm_count() {
     return n;
 }
 
+// Dynamic shared memory a PSF kernel may use: the device's opt-in maximum per block less
+// 1 KB for the kernels' static shared variables (mbarrier, work-queue slot).
 static size_t max_smem_optin() {
     int dev = 0, v = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    return v > 0 ? (size_t)v : 227 * 1024;
+    return (v > 0 ? (size_t)v : 227 * 1024) - 1024;
 }
 
 }  // namespace gb
@@ -567,8 +569,10 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
             free_plan(p);
             return GB_ERR_UNSUPPORTED;
         }
-        FAIL_CUDA(setup_fwd(K, fwd_psf_smem_bytes(K, p->N, p->Zt_fwd, 512), 512));
-        FAIL_CUDA(setup_b1(K, b1_psf_smem_bytes(K, p->N, p->Zt_b1)));
+        // the limit is a property of the kernel, shared by every plan of this tap bucket:
+        // raise it to the device maximum (each launch still asks only for its own tile)
+        FAIL_CUDA(setup_fwd(K, max_smem_optin(), 512));
+        FAIL_CUDA(setup_b1(K, max_smem_optin()));
     } else {
         p->Zt_fwd = p->Zt_b1 = p->nz;
     }
@@ -717,8 +721,8 @@ gb_status gb_spect_set_tuning(gb_spect_plan *p, const gb_spect_tuning *tuning) {
     gb_status st = resolve_tuning(p, t);
     if (st != GB_OK) return st;
     const int K = p->dev.K;
-    GB_CUDA(setup_fwd(K, fwd_psf_smem_bytes(K, p->N, t.fwd_zt, t.fwd_tpb), t.fwd_tpb));
-    GB_CUDA(setup_b1(K, b1_psf_smem_bytes(K, p->N, t.b1_zt)));
+    GB_CUDA(setup_fwd(K, max_smem_optin(), t.fwd_tpb));
+    GB_CUDA(setup_b1(K, max_smem_optin()));
     p->fwd_tpb = t.fwd_tpb;
     p->Zt_fwd = t.fwd_zt;
     p->fwd_items = t.fwd_items;

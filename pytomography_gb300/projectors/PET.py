@@ -113,6 +113,11 @@ class PETLMSystemMatrix(SystemMatrix):
         return torch.ones(tuple(self.object_meta.shape)).to(self.device) * fov
 
     # ------------------------------------------------------------ subsets
+    def set_deterministic(self, on: bool = True) -> None:
+        """Back projections accumulate as 64-bit fixed-point sums (gb_pet_set_deterministic):
+        bit-identical from run to run, equal to the float path to rounding."""
+        _lib.check(self._lib.gb_pet_set_deterministic(self._plan, int(bool(on))))
+
     def set_n_subsets(self, n_subsets: int) -> None:
         idx = torch.arange(self.proj_meta.detector_ids.shape[0]).to(torch.long).cpu()
         self.subset_indices_array = [idx[i::n_subsets] for i in range(n_subsets)]
