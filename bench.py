@@ -295,6 +295,23 @@ def run_pet(args, dev):
 
     fused_ms = _events_timer(fused, args.steps)
     plain_ms = _events_timer(plain, max(10, args.steps // 5))
+    sens_s = None
+    if getattr(args, "pet_sensitivity", False):
+        # the one-time sensitivity image over every crystal pair (C(57600, 2) = 1.66e9
+        # LORs, non-TOF back projection, pairs generated on the device), timed once
+        from pytomography_gb300 import _lib
+        img = torch.empty(w.shape, device=dev)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        _lib.check(H._lib.gb_pet_sensitivity(H._plan, None, 0, None, None, 0.0, _lib.ptr(img),
+                                             _lib.stream_handle(dev)))
+        b.record()
+        torch.cuda.synchronize()
+        n_det = int(H.proj_meta.scanner_lut.shape[0])
+        n_pairs = n_det * (n_det - 1) // 2
+        sens_s = {"seconds": a.elapsed_time(b) / 1000.0, "lors": n_pairs,
+                  "lors_per_s": n_pairs / (a.elapsed_time(b) / 1000.0)}
     fwd_ms = _events_timer(lambda: H.forward(f, 0), 20)
     p0 = H.forward(f, 0)
     bwd_ms = _events_timer(lambda: H.backward(p0, 0), 20)
@@ -327,7 +344,9 @@ def run_pet(args, dev):
             "events_per_s": (E / w.n_subsets) / (fused_ms / 1000.0),
             "plain": {"value": 1000.0 / plain_ms, "ms_per_step": plain_ms},
             "forward_ms": fwd_ms, "backward_ms": bwd_ms, "cpu_baseline": cpu}
-    print(json.dumps(line))
+    if sens_s is not None:
+        line["sensitivity_all_pairs"] = sens_s
+    return line
 
 
 def run_autograd(args, dev):
@@ -367,7 +386,7 @@ def run_autograd(args, dev):
             "config": {"workload": "8 objects x 128^3, 120 angles, att+PSF, autograd",
                        "bsrem": "RDP beta 0.3 gamma 2, 10 subsets"},
             "bsrem": {"value": 1000.0 / bsrem_ms, "unit": "subiter/s", "ms_per_step": bsrem_ms}}
-    print(json.dumps(line))
+    return line
 
 
 def run_serving(args, dev):
@@ -447,57 +466,18 @@ def run_serving(args, dev):
                                 "what": "the reference's per-call GPU sequence restated in "
                                         "plain PyTorch float32, one round of 32"},
             "batched_vs_torch_reference": torch_ref_ms / batch_ms}
-    print(json.dumps(line))
+    return line
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=20)
-    ap.add_argument("--impl", default="gbtomo", choices=["gbtomo", "reference"])
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--out", default=os.path.join(ROOT, "bench_out"),
-                    help="folder for the clock samples of the timed region (clocks.csv)")
-    ap.add_argument("--profile-case", action="store_true",
-                    help="run 3 fused sub-iterations of the workload and exit (for ncu)")
-    ap.add_argument("--workload", default="osem128",  # osem64: the 64^3 / 64-angle att case
-                    choices=["osem128", "osem64", "serving", "pet", "autograd"],
-                    help="osem128: the 128^3 x 120-angle reconstruction (default); serving: "
-                         "32 uneven reconstructions, batched vs plain; pet: TOF listmode OSEM "
-                         "(10M events); autograd: Poisson-NLL gradients of 8 objects + BSREM")
-    args = ap.parse_args()
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    if args.impl == "reference":
-        if rank == 0:
-            run_reference(args)
-        return
-    if args.warmup < 3:
-        args.warmup = 3
-
+def run_osem(args, dev, w, rank, world, dist, full=True):
+    """One OSEM workload: fused sub-iterations from graphs (the line's value), the plain
+    per-call path, the PyTorch restatement of the reference sequence, the forward
+    projector's roofline, end to end through the public API and (full) the CPU baselines."""
     import torch
     from pytomography_gb300 import _lib, synthetic
     from pytomography_gb300.algorithms import OSEM
     from pytomography_gb300.likelihoods import PoissonLogLikelihood
-
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    dev = torch.device("cuda", local)
-    _lib.load()
-    if args.workload == "serving":
-        return run_serving(args, dev)
-    if args.workload == "pet":
-        return run_pet(args, dev)
-    if args.workload == "autograd":
-        return run_autograd(args, dev)
-
-    w = synthetic.config1() if args.workload == "osem64" else synthetic.config2()
-    metric = METRIC if args.workload != "osem64" else "OSEM subiter/s at 64^3x64 ang (att)"
+    metric = METRIC if w.shape[0] == 128 else "OSEM subiter/s at 64^3x64 ang (att)"
     H = synthetic.build_system_matrix(w)
     g_host = synthetic.poisson_projections(H, w)
     g = g_host.to(dev)
@@ -512,7 +492,7 @@ def main():
             H.osem_step(f, g, None, nbps[k], k)
         torch.cuda.synchronize()
         print("profile case done")
-        return
+        return None
 
     # ---- plain per-call path (reference sequence through the drop-in projector)
     def plain_step(k):
@@ -661,6 +641,7 @@ def main():
                      f"angles forward + back projected, scaled to {n_sel}"}
         del Rc
 
+    line = None
     if rank == 0:
         line = {
             "metric": metric, "value": value, "unit": "subiter/s", "n_gpus": world,
@@ -701,6 +682,106 @@ def main():
             "cpu_baseline": cpu,
             "cpu_torch_reference": cpu_torch,
         }
+    return line
+
+
+
+
+def extra_configs(args, dev):
+    """The other benchmark configurations, each timed on its own with CUDA events and
+    reported beside the headline: 64^3 x 64 OSEM, PET TOF listmode OSEM (10M events),
+    Poisson-NLL gradients of 8 objects and BSREM, and the 32-reconstruction serving batch."""
+    from pytomography_gb300 import synthetic
+    import argparse as _ap
+    sub = _ap.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.no_cpu, sub.profile_case = min(args.steps, 50), 3, True, False
+    out = {}
+
+    def keep(line, keys):
+        return {k: line[k] for k in keys if k in line}
+
+    t0 = time.perf_counter()
+    l1 = run_osem(sub, dev, synthetic.config1(), 0, 1, None, full=False)
+    out["osem64"] = keep(l1, ("metric", "value", "unit", "ms_per_step", "plain", "fused_vs_plain",
+                              "e2e", "roofline", "config"))
+    l3 = run_pet(sub, dev)
+    out["pet"] = keep(l3, ("metric", "value", "unit", "ms_per_step", "events_per_s", "plain",
+                           "forward_ms", "backward_ms", "config"))
+    l4 = run_autograd(sub, dev)
+    out["autograd"] = keep(l4, ("metric", "value", "unit", "ms_per_step", "bsrem", "config"))
+    l5 = run_serving(sub, dev)
+    out["serving"] = keep(l5, ("metric", "value", "unit", "ms_per_step", "plain",
+                               "batched_vs_plain", "config"))
+    out["wall_s"] = time.perf_counter() - t0
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gbtomo", choices=["gbtomo", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--out", default=os.path.join(ROOT, "bench_out"),
+                    help="folder for the clock samples of the timed region (clocks.csv)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="report only the 128^3 workload (skip the other configurations)")
+    ap.add_argument("--pet-sensitivity", action="store_true",
+                    help="with --workload pet: also time the all-pairs sensitivity image once")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run 3 fused sub-iterations of the workload and exit (for ncu)")
+    ap.add_argument("--workload", default="osem128",  # osem64: the 64^3 / 64-angle att case
+                    choices=["osem128", "osem64", "serving", "pet", "autograd"],
+                    help="osem128: the 128^3 x 120-angle reconstruction (default); serving: "
+                         "32 uneven reconstructions, batched vs plain; pet: TOF listmode OSEM "
+                         "(10M events); autograd: Poisson-NLL gradients of 8 objects + BSREM")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+
+    import torch
+    from pytomography_gb300 import _lib, synthetic
+    from pytomography_gb300.algorithms import OSEM
+    from pytomography_gb300.likelihoods import PoissonLogLikelihood
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    _lib.load()
+    if args.workload == "serving":
+        return run_serving(args, dev)
+    if args.workload == "pet":
+        return run_pet(args, dev)
+    if args.workload == "autograd":
+        return run_autograd(args, dev)
+
+    if args.workload == "serving":
+        print(json.dumps(run_serving(args, dev)))
+        return
+    if args.workload == "pet":
+        print(json.dumps(run_pet(args, dev)))
+        return
+    if args.workload == "autograd":
+        print(json.dumps(run_autograd(args, dev)))
+        return
+    w = synthetic.config1() if args.workload == "osem64" else synthetic.config2()
+    line = run_osem(args, dev, w, rank, world, dist, full=True)
+    if args.profile_case:
+        return
+    if rank == 0 and world == 1 and args.workload == "osem128" and not args.headline_only:
+        line["configs"] = extra_configs(args, dev)
+    if rank == 0:
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

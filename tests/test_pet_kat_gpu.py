@@ -49,10 +49,12 @@ def test_uniform_box_oblique_chords(cuda):
             a, b = (k + 1) % 3, (k + 2) % 3
             p0, p1 = np.zeros(3), np.zeros(3)
             p0[k], p1[k] = -400.0, 400.0
-            # stay at least one voxel inside the box along the other two axes
+            # stay at least one voxel inside the box along the other two axes, with slopes
+            # below 1/2 so that k stays the principal axis
             for ax in (a, b):
                 m = half[ax] - 1.5 * vox[ax]
-                c0, c1 = rng.uniform(-m, m, 2)
+                c0 = rng.uniform(-m, m)
+                c1 = float(np.clip(c0 + rng.uniform(-0.9, 0.9) * half[k], -m, m))
                 # the LOR's value on this axis over the box's extent along k
                 slope = (c1 - c0) / (2 * half[k])
                 p0[ax] = c0 - slope * (400.0 - half[k])
