@@ -759,12 +759,6 @@ def main():
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     _lib.load()
-    if args.workload == "serving":
-        return run_serving(args, dev)
-    if args.workload == "pet":
-        return run_pet(args, dev)
-    if args.workload == "autograd":
-        return run_autograd(args, dev)
 
     if args.workload == "serving":
         print(json.dumps(run_serving(args, dev)))
