@@ -124,6 +124,10 @@ typedef struct gb_spect_tuning {
     int32_t fwd_items; /* forward work items per resident CTA slot and z slab: 1 or 2 */
     int32_t b1_zt;     /* back-projection (rotated frame) z-slab width; 0 = widest */
     int32_t b1_items;  /* back-projection work items per SM and z slab: 1 or 2 */
+    int32_t fwd_variant; /* forward kernel: 1 (samples gathered per plane, y blur first) or 2
+                            (corner rows staged through a cp.async ring, z blur first;
+                            attenuation before a 2-D PSF of at most 29 taps, N and
+                            nz <= 128); 0 keeps the plan's current one */
 } gb_spect_tuning;
 gb_status gb_spect_get_tuning(const gb_spect_plan *plan, gb_spect_tuning *out);
 /* Apply a tuning (rebuilds the work lists of the current subsets; may allocate: call at

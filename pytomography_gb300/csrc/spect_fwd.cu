@@ -10,6 +10,7 @@
 
 #include <cstring>
 
+#include "spect_fwd_v2.cuh"
 #include "spect_kernels.cuh"
 #include "spect_launch.h"
 
@@ -23,6 +24,13 @@ namespace gb {
     cudaError_t setup_fwd_##KK(size_t smem, int tpb);
 GB_FOR_EACH_K(GB_DECL_FWD)
 #undef GB_DECL_FWD
+#define GB_DECL_FWD2(KK)                                                                     \
+    cudaError_t setup_fwd2_##KK();                                                           \
+    cudaError_t launch_fwd2_##KK(const SpectDev &g, const float *f, const int *alist,        \
+                                 const int4 *items, int n_items, float *partials,            \
+                                 cudaStream_t st);
+GB_FOR_EACH_K2(GB_DECL_FWD2)
+#undef GB_DECL_FWD2
 
 // ------------------------------------------------------------- without PSF
 // One thread per output (y, z) of an item's planes, or per (y, z quad) with nz % 4 == 0;
@@ -208,8 +216,38 @@ cudaError_t setup_fwd(int K, size_t smem, int tpb) {
     }
 }
 
+bool fwd2_eligible(const SpectDev &g, size_t smem_cap) {
+    return g.psf && g.psf2d && g.att && g.att_first && g.A && g.K <= kFwd2MaxK &&
+           g.N <= 128 && g.nz <= 128 && g.nz % 4 == 0 &&
+           fwd2_smem_floats(g.K, g.N, g.nz) * sizeof(float) <= smem_cap;
+}
+
+cudaError_t setup_fwd2(int K) {
+    switch (K) {
+#define GB_SETUP2_CASE(KK) \
+    case KK:               \
+        return setup_fwd2_##KK();
+        GB_FOR_EACH_K2(GB_SETUP2_CASE)
+#undef GB_SETUP2_CASE
+        default:
+            return cudaErrorNotSupported;
+    }
+}
+
 cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, const int4 *items,
-                       int n_items, int Zt, int tpb, float *partials, cudaStream_t st) {
+                       int n_items, int Zt, int tpb, int variant, float *partials,
+                       cudaStream_t st) {
+    if (variant == 2 && g.psf) {
+        switch (g.K) {
+#define GB_FWD2_CASE(KK) \
+    case KK:             \
+        return launch_fwd2_##KK(g, f, alist, items, n_items, partials, st);
+            GB_FOR_EACH_K2(GB_FWD2_CASE)
+#undef GB_FWD2_CASE
+            default:
+                return cudaErrorNotSupported;
+        }
+    }
     if (!g.psf) {
         if (g.nz % 4 == 0) {
             dim3 grid(n_items, (g.N * (g.nz / 4) + 255) / 256);

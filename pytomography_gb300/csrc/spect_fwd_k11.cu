@@ -4,5 +4,6 @@
 namespace gb {
 
 GB_FWD_PSF_INSTANCE(11)
+GB_FWD2_INSTANCE(11)
 
 }  // namespace gb

@@ -4,5 +4,6 @@
 namespace gb {
 
 GB_FWD_PSF_INSTANCE(15)
+GB_FWD2_INSTANCE(15)
 
 }  // namespace gb

@@ -4,5 +4,6 @@
 namespace gb {
 
 GB_FWD_PSF_INSTANCE(21)
+GB_FWD2_INSTANCE(21)
 
 }  // namespace gb

@@ -4,5 +4,6 @@
 namespace gb {
 
 GB_FWD_PSF_INSTANCE(25)
+GB_FWD2_INSTANCE(25)
 
 }  // namespace gb

@@ -4,5 +4,6 @@
 namespace gb {
 
 GB_FWD_PSF_INSTANCE(7)
+GB_FWD2_INSTANCE(7)
 
 }  // namespace gb

@@ -15,6 +15,7 @@
 #pragma once
 #include "spect_blur.cuh"
 #include "spect_kernels.cuh"
+#include "spect_fwd_v2.cuh"
 #include "spect_launch.h"
 
 namespace gb {
@@ -614,6 +615,16 @@ inline cudaError_t setup_fwd_t(size_t smem) {
     }                                                                                        \
     cudaError_t setup_fwd_##KK(size_t smem, int tpb) {                                       \
         return tpb <= 512 ? setup_fwd_t<KK, 512>(smem) : setup_fwd_t<KK, 768>(smem);         \
+    }
+
+// Entry points of the second forward variant for one tap bucket (spect_fwd_k*.cu, the
+// buckets of GB_FOR_EACH_K2).
+#define GB_FWD2_INSTANCE(KK)                                                                 \
+    cudaError_t setup_fwd2_##KK() { return setup_fwd2_t<KK>(); }                             \
+    cudaError_t launch_fwd2_##KK(const SpectDev &g, const float *f, const int *alist,        \
+                                 const int4 *items, int n_items, float *partials,            \
+                                 cudaStream_t st) {                                          \
+        return launch_fwd2_t<KK>(g, f, alist, items, n_items, partials, st);                 \
     }
 
 }  // namespace gb

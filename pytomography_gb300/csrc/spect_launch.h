@@ -8,6 +8,8 @@
 // PSF tap-count buckets compiled into the library: a plan's taps are zero-padded
 // (centred) to the smallest bucket that holds its widest kernel.
 #define GB_FOR_EACH_K(X) X(7) X(11) X(15) X(21) X(25) X(29) X(37) X(45)
+// the buckets the second forward variant (k_fwd_psf2) is compiled for
+#define GB_FOR_EACH_K2(X) X(7) X(11) X(15) X(21) X(25) X(29)
 
 namespace gb {
 
@@ -34,8 +36,13 @@ cudaError_t setup_b1(int K, size_t smem);
 
 // Work items (int4: slot, first plane, end plane, unused) split each angle's planes
 // into ranges of about equal work; partial sums are indexed by item.
+// variant 1: k_fwd_psf (tpb 512 or 768); variant 2: k_fwd_psf2 (cp.async ring, z blur first;
+// attenuation before a 2-D PSF, N <= 128, nz <= 128, nz % 4 == 0, at most 29 taps)
 cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, const int4 *items,
-                       int n_items, int Zt, int tpb, float *partials, cudaStream_t st);
+                       int n_items, int Zt, int tpb, int variant, float *partials,
+                       cudaStream_t st);
+bool fwd2_eligible(const SpectDev &g, size_t smem_cap);
+cudaError_t setup_fwd2(int K);
 // ioff[slot] .. ioff[slot+1]: the items of a slot
 cudaError_t launch_reduce(int n_slots, const int *ioff, int NZ, const float *partials, float *out,
                           int ratio, const float *gproj, const float *sadd, const int *alist,
@@ -136,6 +143,7 @@ struct FwdArgs {
     const int *ioff;
     int Zt;
     int tpb;
+    int variant;
 };
 bool plan_forward_args(const gb_spect_plan *p, int subset, FwdArgs *a);
 

@@ -122,6 +122,7 @@ struct gb_spect_plan {
     int *d_err = nullptr;
     int Zt_fwd = 0, Zt_b1 = 0;
     int fwd_tpb = 512;  // forward CTA size: 512 or 768 threads (one CTA per SM)
+    int fwd_variant = 1;  // 1: k_fwd_psf; 2: k_fwd_psf2
     int fwd_items = 1, b1_items = 1;  // work items per resident CTA slot and z slab
     unsigned lists_version = 0;       // bumped whenever the subset / work lists change
 };
@@ -685,6 +686,7 @@ gb_status gb_spect_get_tuning(const gb_spect_plan *p, gb_spect_tuning *out) {
     clear_error();
     GB_CHECK_ARG(p && out, "null argument");
     out->fwd_tpb = p->fwd_tpb;
+    out->fwd_variant = p->fwd_variant;
     out->fwd_zt = p->Zt_fwd;
     out->fwd_items = p->fwd_items;
     out->b1_zt = p->Zt_b1;
@@ -696,6 +698,13 @@ gb_status gb_spect_get_tuning(const gb_spect_plan *p, gb_spect_tuning *out) {
 static gb_status resolve_tuning(const gb_spect_plan *p, gb_spect_tuning &t) {
     const int K = p->dev.K, OB = (K <= 31) ? 8 : 4;
     GB_CHECK_ARG(t.fwd_tpb == 512 || t.fwd_tpb == 768, "fwd_tpb must be 512 or 768");
+    if (t.fwd_variant == 0) t.fwd_variant = p->fwd_variant;
+    GB_CHECK_ARG(t.fwd_variant == 1 || t.fwd_variant == 2, "fwd_variant must be 1 or 2");
+    if (t.fwd_variant == 2 && !fwd2_eligible(p->dev, max_smem_optin())) {
+        set_error("forward variant 2 needs attenuation before a 2-D PSF of at most 29 taps, "
+                  "N and nz <= 128 and nz %% 4 == 0");
+        return GB_ERR_UNSUPPORTED;
+    }
     GB_CHECK_ARG(t.fwd_items >= 1 && t.fwd_items <= 2 && t.b1_items >= 1 && t.b1_items <= 2,
                  "items per SM must be 1 or 2");
     const int zf = choose_zt(K, p->N, p->nz, true, t.fwd_tpb);
@@ -704,9 +713,10 @@ static gb_status resolve_tuning(const gb_spect_plan *p, gb_spect_tuning &t) {
         set_error("the %d-thread forward tile does not fit shared memory", t.fwd_tpb);
         return GB_ERR_UNSUPPORTED;
     }
-    if (t.fwd_zt == 0) t.fwd_zt = zf;
+    if (t.fwd_zt == 0 || t.fwd_variant == 2) t.fwd_zt = t.fwd_variant == 2 ? p->nz : zf;
     if (t.b1_zt == 0) t.b1_zt = zb;
-    GB_CHECK_ARG(t.fwd_zt > 0 && t.fwd_zt <= zf && (t.fwd_zt % OB == 0 || t.fwd_zt == p->nz),
+    GB_CHECK_ARG(t.fwd_variant == 2 ||
+                     (t.fwd_zt > 0 && t.fwd_zt <= zf && (t.fwd_zt % OB == 0 || t.fwd_zt == p->nz)),
                  "fwd_zt must be a multiple of %d in (0, %d]", OB, zf);
     GB_CHECK_ARG(t.b1_zt > 0 && t.b1_zt <= zb && (t.b1_zt % OB == 0 || t.b1_zt == p->nz),
                  "b1_zt must be a multiple of %d in (0, %d]", OB, zb);
@@ -723,7 +733,9 @@ gb_status gb_spect_set_tuning(gb_spect_plan *p, const gb_spect_tuning *tuning) {
     const int K = p->dev.K;
     GB_CUDA(setup_fwd(K, max_smem_optin(), t.fwd_tpb));
     GB_CUDA(setup_b1(K, max_smem_optin()));
+    if (t.fwd_variant == 2) GB_CUDA(setup_fwd2(K));
     p->fwd_tpb = t.fwd_tpb;
+    p->fwd_variant = t.fwd_variant;
     p->Zt_fwd = t.fwd_zt;
     p->fwd_items = t.fwd_items;
     p->Zt_b1 = t.b1_zt;
@@ -742,7 +754,7 @@ static gb_status run_forward(gb_spect_plan *p, const float *obj, int subset, flo
     const gb_spect_plan::List &L = p->lists[li];
     const int *alist = p->d_alist + L.alist_off;
     GB_CUDA(launch_fwd(p->dev, obj, alist, p->d_items + L.fitem_off, L.n_fitems, p->Zt_fwd,
-                       p->fwd_tpb, p->d_partials, st));
+                       p->fwd_tpb, p->fwd_variant, p->d_partials, st));
     GB_CUDA(launch_reduce(L.n, p->d_ioff + L.ioff_off, p->N * p->nz, p->d_partials, out, ratio,
                           gproj, sadd, alist, pred, st));
     return GB_OK;
@@ -879,6 +891,7 @@ gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
             if (zt < 2 * OB || (zt != zmax && zt >= p->nz)) continue;
             for (int items : {1, 2}) {
                 gb_spect_tuning t = best;
+                t.fwd_variant = 1;
                 t.fwd_tpb = tpb;
                 t.fwd_zt = zt;
                 t.fwd_items = items;
@@ -891,9 +904,23 @@ gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
             }
         }
     }
+    if (fwd2_eligible(p->dev, max_smem_optin()))
+        for (int items : {1, 2}) {
+            gb_spect_tuning t = best;
+            t.fwd_variant = 2;
+            t.fwd_tpb = 512;
+            t.fwd_items = items;
+            if (gb_spect_set_tuning(p, &t) != GB_OK) continue;
+            const float ms = time_ms(fwd_call);
+            if (ms >= 0.f && ms < best_ms) {
+                best_ms = ms;
+                fbest = t;
+            }
+        }
     best.fwd_tpb = fbest.fwd_tpb;
     best.fwd_zt = fbest.fwd_zt;
     best.fwd_items = fbest.fwd_items;
+    best.fwd_variant = fbest.fwd_variant;
     // back-projection candidates (with the chosen forward tiles)
     best_ms = 1e30f;
     gb_spect_tuning bbest = best;
@@ -1052,6 +1079,7 @@ bool plan_forward_args(const gb_spect_plan *p, int subset, FwdArgs *a) {
     a->ioff = p->d_ioff + L.ioff_off;
     a->Zt = p->Zt_fwd;
     a->tpb = p->fwd_tpb;
+    a->variant = p->fwd_variant;
     return true;
 }
 

@@ -76,7 +76,8 @@ extern "C" gb_status gb_spect_forward_static(gb_spect_plan *plan, const float *o
     gb_status s = static_scratch(&scratch);
     if (s != GB_OK) return s;
     cudaStream_t st = as_stream(stream);
-    GB_CUDA(launch_fwd(a.g, object, a.alist, a.items, a.n_items, a.Zt, a.tpb, scratch, st));
+    GB_CUDA(launch_fwd(a.g, object, a.alist, a.items, a.n_items, a.Zt, a.tpb, a.variant, scratch,
+                       st));
     GB_CUDA(launch_reduce(a.n_sel, a.ioff, a.g.N * a.g.nz, scratch, proj, 0, nullptr, nullptr,
                           a.alist, nullptr, st));
     return GB_OK;

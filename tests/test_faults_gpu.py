@@ -47,6 +47,7 @@ def test_injected_allocation_failure_on_gpu(cuda):
 
 def test_bounded_wait_runs_out_and_reports(cuda):
     d, H, f = _sm(cuda, check_device_status=True)
+    H.set_tuning(fwd_variant=1)  # the forward with TMA attenuation copies and bounded waits
     assert H.device_status() == 0
     # every work item's first attenuation copy is left unissued; each wait gives up after
     # 16 polls of at most 20 us

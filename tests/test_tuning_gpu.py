@@ -87,3 +87,37 @@ def test_invalid_tunings_raise(cuda):
         H.set_tuning(fwd_zt=5)  # not a multiple of the output block
     with pytest.raises(RuntimeError):
         H.set_tuning(b1_zt=4096)
+
+
+@pytest.mark.parametrize("n,nz,n_angles", [(128, 128, 24), (96, 96, 30), (64, 64, 20),
+                                           (128, 100, 12), (40, 24, 10)])
+def test_forward_variant2_matches_oracle_and_variant1(n, nz, n_angles, cuda):
+    """The cp.async-ring forward (z blur first) against the oracle per projection and
+    against the first variant, for one and two work items per CTA slot."""
+    H, o, f = _geometry(n=n, nz=nz, n_angles=n_angles)
+    H.set_n_subsets(2)
+    idx = H.subset_indices_array[1].cpu().numpy()
+    ref = o.forward(f, idx)
+    ft = torch.tensor(f, dtype=torch.float32, device=cuda)
+    H.set_tuning(fwd_variant=1)
+    v1 = H.forward(ft, 1).cpu().numpy()
+    for items in (1, 2):
+        H.set_tuning(fwd_variant=2, fwd_items=items)
+        assert H.get_tuning()["fwd_variant"] == 2
+        v2 = H.forward(ft, 1).cpu().numpy()
+        for a in range(v2.shape[0]):
+            assert rel_l2(v2[a], ref[a]) < TOL, (items, a)
+        assert rel_l2(v2, v1) < TOL
+        assert np.array_equal(v2, H.forward(ft, 1).cpu().numpy())  # deterministic
+    assert H.device_status() == 0
+
+
+def test_forward_variant2_rejected_where_it_does_not_apply(cuda):
+    from pytomography_gb300.metadata.SPECT import SPECTObjectMeta, SPECTProjMeta, SPECTPSFMeta
+    from pytomography_gb300.projectors.SPECT import SPECTSystemMatrix
+    from pytomography_gb300.transforms.SPECT import SPECTPSFTransform
+    om = SPECTObjectMeta([0.442] * 3, (32, 32, 16))
+    pm = SPECTProjMeta((32, 16), [0.442] * 2, [0.0, 90.0], radii=[22.0, 22.0])
+    H = SPECTSystemMatrix([SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)))], [], om, pm)
+    with pytest.raises(RuntimeError, match="variant 2"):
+        H.set_tuning(fwd_variant=2)  # no attenuation
