@@ -738,6 +738,9 @@ def main():
                     help="report only the 128^3 workload (skip the other configurations)")
     ap.add_argument("--pet-sensitivity", action="store_true",
                     help="with --workload pet: also time the all-pairs sensitivity image once")
+    ap.add_argument("--profile-forward", type=int, default=0, choices=[0, 1, 2],
+                    help="run three 12-angle forward projections of the 128^3 workload with "
+                         "forward variant 1 or 2 and exit (for ncu)")
     ap.add_argument("--profile-case", action="store_true",
                     help="run 3 fused sub-iterations of the workload and exit (for ncu)")
     ap.add_argument("--workload", default="osem128",  # osem64: the 64^3 / 64-angle att case
@@ -769,6 +772,17 @@ def main():
     dev = torch.device("cuda", local)
     _lib.load()
 
+    if args.profile_forward:
+        w = synthetic.config2()
+        H = synthetic.build_system_matrix(w)
+        H.set_n_subsets(w.n_subsets)
+        H.set_tuning(fwd_variant=args.profile_forward)
+        f = torch.tensor(w.activity, dtype=torch.float32, device=dev)
+        for k in range(3):
+            H.forward(f, k)
+        torch.cuda.synchronize()
+        print("profile forward done", args.profile_forward)
+        return
     if args.workload == "serving":
         line = run_serving(args, dev)
         if not args.profile_case:

@@ -128,6 +128,9 @@ typedef struct gb_spect_tuning {
                             (corner rows staged through a cp.async ring, z blur first;
                             attenuation before a 2-D PSF of at most 29 taps, N and
                             nz <= 128); 0 keeps the plan's current one */
+    int32_t osem_split;  /* 1: gb_spect_osem_step runs the two halves of a subset's angles on
+                            two streams (fork / join by events, same kernels and results);
+                            0: one stream */
 } gb_spect_tuning;
 gb_status gb_spect_get_tuning(const gb_spect_plan *plan, gb_spect_tuning *out);
 /* Apply a tuning (rebuilds the work lists of the current subsets; may allocate: call at

@@ -37,7 +37,7 @@ class SpectDesc(ctypes.Structure):
 
 class SpectTuning(ctypes.Structure):
     _fields_ = [("fwd_tpb", c_int), ("fwd_zt", c_int), ("fwd_items", c_int), ("b1_zt", c_int),
-                ("b1_items", c_int), ("fwd_variant", c_int)]
+                ("b1_items", c_int), ("fwd_variant", c_int), ("osem_split", c_int)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -109,6 +109,7 @@ struct gb_spect_plan {
         int fitem_off = 0, n_fitems = 0;  // forward items in d_items
         int ioff_off = 0;                 // n + 1 item offsets per slot in d_ioff
         std::vector<int> gitem_off, n_gitems;  // B1 items of each angle group
+        int f_half = 0, b_half = 0;  // first forward / group-0 B1 item of slot n / 2
     };
     std::vector<List> lists;
     std::vector<float> h_theta_fwd, h_lin;
@@ -125,6 +126,11 @@ struct gb_spect_plan {
     int fwd_variant = 1;  // 1: k_fwd_psf; 2: k_fwd_psf2
     int fwd_items = 1, b1_items = 1;  // work items per resident CTA slot and z slab
     unsigned lists_version = 0;       // bumped whenever the subset / work lists change
+    // fused OSEM step in two angle halves on two streams (the second half's forward and
+    // the first half's back projection overlap; fork / join by events)
+    int osem_split = 1;
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 static void free_plan(gb_spect_plan *p) {
@@ -138,6 +144,9 @@ static void free_plan(gb_spect_plan *p) {
     cudaFree(p->d_bp);
     cudaFree(p->d_wrange);
     cudaFree(p->d_err);
+    if (p->st2) cudaStreamDestroy(p->st2);
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
     delete p;
 }
 
@@ -316,6 +325,7 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
             std::vector<int> cnt = chunk_counts(p, wa, zs_f, p->fwd_items);
             for (int i = 0; i < L.n; i++) {
                 ioff.push_back((int)items.size() - L.fitem_off);
+                if (i == L.n / 2) L.f_half = (int)items.size() - L.fitem_off;
                 split_planes(wf[l[i]], cnt[i], i, items);
             }
         } else {
@@ -337,7 +347,10 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
                 std::vector<double> wa(na);
                 for (int i = 0; i < na; i++) wa[i] = sum_of(wb[l[a0 + i]]);
                 std::vector<int> cnt = chunk_counts(p, wa, zs_b, p->b1_items);
-                for (int i = 0; i < na; i++) split_planes(wb[l[a0 + i]], cnt[i], i, items);
+                for (int i = 0; i < na; i++) {
+                    if (a0 == 0 && i == L.n / 2) L.b_half = (int)items.size() - L.gitem_off.back();
+                    split_planes(wb[l[a0 + i]], cnt[i], i, items);
+                }
             }
             L.n_gitems.push_back((int)items.size() - L.gitem_off.back());
         }
@@ -600,6 +613,9 @@ gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     FAIL_CUDA(cudaMemset(p->d_wrange, 0, (size_t)p->G * Lp * sizeof(int2)));
     FAIL_CUDA(dev_alloc(&p->d_err, sizeof(int)));
     FAIL_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+    FAIL_CUDA(cudaStreamCreateWithFlags(&p->st2, cudaStreamNonBlocking));
+    FAIL_CUDA(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+    FAIL_CUDA(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
     g.wrange = p->d_wrange;
     g.err = p->d_err;
 #undef FAIL_CUDA
@@ -687,6 +703,7 @@ gb_status gb_spect_get_tuning(const gb_spect_plan *p, gb_spect_tuning *out) {
     GB_CHECK_ARG(p && out, "null argument");
     out->fwd_tpb = p->fwd_tpb;
     out->fwd_variant = p->fwd_variant;
+    out->osem_split = p->osem_split;
     out->fwd_zt = p->Zt_fwd;
     out->fwd_items = p->fwd_items;
     out->b1_zt = p->Zt_b1;
@@ -700,6 +717,7 @@ static gb_status resolve_tuning(const gb_spect_plan *p, gb_spect_tuning &t) {
     GB_CHECK_ARG(t.fwd_tpb == 512 || t.fwd_tpb == 768, "fwd_tpb must be 512 or 768");
     if (t.fwd_variant == 0) t.fwd_variant = p->fwd_variant;
     GB_CHECK_ARG(t.fwd_variant == 1 || t.fwd_variant == 2, "fwd_variant must be 1 or 2");
+    GB_CHECK_ARG(t.osem_split == 0 || t.osem_split == 1, "osem_split must be 0 or 1");
     if (t.fwd_variant == 2 && !fwd2_eligible(p->dev, max_smem_optin())) {
         set_error("forward variant 2 needs attenuation before a 2-D PSF of at most 29 taps, "
                   "N and nz <= 128 and nz %% 4 == 0");
@@ -736,6 +754,7 @@ gb_status gb_spect_set_tuning(gb_spect_plan *p, const gb_spect_tuning *tuning) {
     if (t.fwd_variant == 2) GB_CUDA(setup_fwd2(K));
     p->fwd_tpb = t.fwd_tpb;
     p->fwd_variant = t.fwd_variant;
+    p->osem_split = t.osem_split;
     p->Zt_fwd = t.fwd_zt;
     p->fwd_items = t.fwd_items;
     p->Zt_b1 = t.b1_zt;
@@ -953,6 +972,43 @@ gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
     return rc;
 }
 
+// The fused OSEM sub-iteration in two halves of the subset's angles (one angle group):
+// half A's forward, reduction and B1 on the caller's stream, half B's on the plan's second
+// stream, then the gather with the update on the caller's stream.  Both forwards start
+// together (one wave of CTAs between them); each half's B1 starts as soon as its own
+// ratio rows exist, filling the SMs the slower forward CTAs leave idle.  The kernels and
+// their work items are the single-stream step's, so results are identical.
+static gb_status osem_split_step(gb_spect_plan *p, const gb_spect_plan::List &L, float *obj,
+                                 const float *g, const float *s, const float *nbp, float *pred,
+                                 cudaStream_t st) {
+    const int *alist = p->d_alist + L.alist_off;
+    const int h = L.n / 2;
+    const size_t NZ = (size_t)p->N * p->nz;
+    const int4 *fit = p->d_items + L.fitem_off;
+    const int *ioff = p->d_ioff + L.ioff_off;
+    const int4 *bit = p->d_items + L.gitem_off[0];
+    cudaStream_t s2 = p->st2;
+    GB_CUDA(cudaEventRecord(p->ev_fork, st));
+    GB_CUDA(cudaStreamWaitEvent(s2, p->ev_fork, 0));
+    GB_CUDA(launch_fwd(p->dev, obj, alist, fit, L.f_half, p->Zt_fwd, p->fwd_tpb, p->fwd_variant,
+                       p->d_partials, st));
+    GB_CUDA(launch_fwd(p->dev, obj, alist, fit + L.f_half, L.n_fitems - L.f_half, p->Zt_fwd,
+                       p->fwd_tpb, p->fwd_variant, p->d_partials + (size_t)L.f_half * NZ, s2));
+    GB_CUDA(launch_reduce(h, ioff, (int)NZ, p->d_partials, p->d_ratio, 1, g, s, alist, pred, st));
+    GB_CUDA(launch_reduce(L.n - h, ioff + h, (int)NZ, p->d_partials, p->d_ratio + h * NZ, 1, g, s,
+                          alist + h, pred ? pred + h * NZ : nullptr, s2));
+    GB_CUDA(launch_b1(p->dev, p->d_ratio, alist, L.n, bit, L.b_half, p->Zt_b1, p->d_W, st));
+    GB_CUDA(launch_b1(p->dev, p->d_ratio, alist, L.n, bit + L.b_half, L.n_gitems[0] - L.b_half,
+                      p->Zt_b1, p->d_W, s2));
+    GB_CUDA(cudaEventRecord(p->ev_join, s2));
+    GB_CUDA(cudaStreamWaitEvent(st, p->ev_join, 0));
+    UpdateArgs u{};
+    u.f = obj;
+    u.nbp = nbp;
+    GB_CUDA(launch_b2_gather(p->dev, p->d_W, alist, L.n, obj, B2_OSEM, u, st));
+    return GB_OK;
+}
+
 gb_status gb_spect_osem_step(gb_spect_plan *p, float *obj, const float *g, const float *s,
                              const float *nbp, int32_t subset, float *pred,
                              gb_stream_t stream) {
@@ -961,12 +1017,15 @@ gb_status gb_spect_osem_step(gb_spect_plan *p, float *obj, const float *g, const
     GB_CHECK_ARG(p && obj && g && nbp, "null argument");
     GB_INJECT_LAUNCH();
     cudaStream_t st = as_stream(stream);
+    const int li = list_index(p, subset);
+    if (li >= 0 && p->osem_split && p->dev.psf && p->lists[li].n >= 4 && p->lists[li].n <= p->G)
+        return osem_split_step(p, p->lists[li], obj, g, s, nbp, pred, st);
     gb_status r = run_forward(p, obj, subset, p->d_ratio, 1, g, s, pred, st);
     if (r != GB_OK) return r;
     UpdateArgs u{};
     u.f = obj;
     u.nbp = nbp;
-    return run_backward(p, p->d_ratio, list_index(p, subset), 0, obj, B2_OSEM, u, st);
+    return run_backward(p, p->d_ratio, li, 0, obj, B2_OSEM, u, st);
 }
 
 static void rdp_weights(float dx, float dy, float dz, float w[26]) {
