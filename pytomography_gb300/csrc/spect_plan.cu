@@ -128,7 +128,7 @@ struct gb_spect_plan {
     unsigned lists_version = 0;       // bumped whenever the subset / work lists change
     // fused OSEM step in two angle halves on two streams (the second half's forward and
     // the first half's back projection overlap; fork / join by events)
-    int osem_split = 1;
+    int osem_split = 0;  // measured slower at 128^3 x 12 angles: off by default
     cudaStream_t st2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
