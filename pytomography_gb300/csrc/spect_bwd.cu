@@ -254,18 +254,23 @@ __device__ __forceinline__ void b1_psf_item(const SpectDev &g, const float *__re
         {
             float *Wp = Ws + (size_t)xp * g.nya * nz;
             const bool amul = Ap && g.att_first;
-            // warp-tasks (32-row chunk, two z blocks of OP): lanes 0-15 and 16-31 take the
-            // 16 row pairs of the chunk for z blocks 2q and 2q + 1
-            const int nrc = ((b_hi - b_lo) * OB + 31) >> 5;
-            const int nzb = Z8 / OP, nzq = (nzb + 1) >> 1;
-            const int half = lane >> 4, pr = lane & 15;
+            // warp-tasks (RP row pairs, 32 consecutive z): lane = (row pair lane % RP, z block
+            // lane / RP of OP values).  Each A load and W store instruction of a warp then
+            // touches RP row pairs x 128 contiguous bytes (4 cache lines per row), not one
+            // 16-byte piece in each of 16 rows; the float2 reads of Tt stay free of bank
+            // conflicts within each half warp (z blocks OP * TS floats apart)
+            constexpr int RP = OP, ZQ = 32 / RP;
+            static_assert(ZQ * OP == 32, "a warp task spans 32 z values");
+            const int nrg = ((b_hi - b_lo) * OB + 2 * RP - 1) / (2 * RP);
+            const int nzb = Z8 / OP, nzg = (nzb + ZQ - 1) / ZQ;
+            const int pr = lane % RP, zq = lane / RP;
             tier_dispatch<K>(tier, [&](auto kk) {
                 constexpr int KK = decltype(kk)::value;
                 float w[KK];
                 load_taps<K, KK>(tap + K, w);
-                for (int p = warp; p < nrc * nzq; p += nwarp) {
-                    const int rc = p % nrc, zb = 2 * (p / nrc) + half;
-                    const int o_row = b_lo * OB + (rc << 5) + 2 * pr;  // rows o_row, o_row + 1
+                for (int p = warp; p < nrg * nzg; p += nwarp) {
+                    const int rg = p % nrg, zb = (p / nrg) * ZQ + zq;
+                    const int o_row = b_lo * OB + rg * 2 * RP + 2 * pr;  // rows o_row, o_row + 1
                     if (o_row >= b_hi * OB || zb >= nzb) continue;
                     const int y = g.pad - H + o_row;
                     const bool st0 = y >= ra && y <= rb, st1 = y + 1 >= ra && y + 1 <= rb;
