@@ -794,17 +794,131 @@ __device__ __forceinline__ float4 b2_gather_sum4(const SpectDev &g, const float 
     return bp;
 }
 
+// The back-rotation samples of a block's (x, y) rows are the same for every z quad of a
+// row: the block computes them once per (row, slot) into shared memory, and each thread
+// then reads its row's entries (broadcast loads) instead of repeating the rotation, the
+// bilinear weights and the row-range tests per thread.  An entry holds the W slab offset
+// of the north-west corner (z excluded), the mask of the corners inside the rows B1
+// wrote (bit 0 nw, 1 ne, 2 sw, 3 se) and the four bilinear weights.  Sums and products
+// are the ones of b2_gather_sum4, in the same order.
+struct __align__(16) B2Tap {
+    int off, mask, pad0, pad1;
+    float nw, ne, sw, se;
+};
+constexpr int kB2Taps = 512;  // entries of one block's table (16 KB)
+
+__device__ __forceinline__ void b2_make_tap(const SpectDev &g, const int *__restrict__ alist,
+                                            int s, int x, int y, B2Tap &t) {
+    float ix, iy;
+    rot_coords(g.theta_bwd + 6 * alist[s], g.lin[x + g.pad], g.lin[y + g.pad], g.half, ix, iy);
+    const Bilin b = bilin(ix, iy);
+    const int r = b.r0, c = b.c0 - g.ya_lo;
+    const int2 *wr = g.wrange + (size_t)s * g.Lp;
+    const bool r0 = (unsigned)r < (unsigned)g.Lp, r1 = (unsigned)(r + 1) < (unsigned)g.Lp;
+    const int2 g0 = r0 ? wr[r] : make_int2(0, 0);
+    const int2 g1 = r1 ? wr[r + 1] : make_int2(0, 0);
+    int m = 0;
+    if (r0 && c >= g0.x && c < g0.y) m |= 1;
+    if (r0 && c + 1 >= g0.x && c + 1 < g0.y) m |= 2;
+    if (r1 && c >= g1.x && c < g1.y) m |= 4;
+    if (r1 && c + 1 >= g1.x && c + 1 < g1.y) m |= 8;
+    t.off = (r * g.nya + c) * g.nz;  // the slab has fewer than 2^31 elements (b2_tab_fits)
+    t.mask = m;
+    t.pad0 = t.pad1 = 0;
+    t.nw = b.nw;
+    t.ne = b.ne;
+    t.sw = b.sw;
+    t.se = b.se;
+}
+
+__device__ __forceinline__ bool b2_tab_fits(const SpectDev &g, int n_rows, int n_slots) {
+    return n_rows * n_slots <= kB2Taps && (long long)g.Lp * g.nya * g.nz < (1LL << 31);
+}
+
+__device__ __forceinline__ float4 b2_tap_sample(const float *__restrict__ Ws, const B2Tap &t,
+                                                int nya, int nz, int z) {
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (t.mask == 0) return zero;
+    const float *p = Ws + t.off + z;
+    const int rs = nya * nz;
+    const float4 vnw = (t.mask & 1) ? __ldg(reinterpret_cast<const float4 *>(p)) : zero;
+    const float4 vne = (t.mask & 2) ? __ldg(reinterpret_cast<const float4 *>(p + nz)) : zero;
+    const float4 vsw = (t.mask & 4) ? __ldg(reinterpret_cast<const float4 *>(p + rs)) : zero;
+    const float4 vse = (t.mask & 8) ? __ldg(reinterpret_cast<const float4 *>(p + rs + nz)) : zero;
+    Bilin b;
+    b.nw = t.nw;
+    b.ne = t.ne;
+    b.sw = t.sw;
+    b.se = t.se;
+    float4 o;
+    o.x = bilin_combine(b, vnw.x, vne.x, vsw.x, vse.x);
+    o.y = bilin_combine(b, vnw.y, vne.y, vsw.y, vse.y);
+    o.z = bilin_combine(b, vnw.z, vne.z, vsw.z, vse.z);
+    o.w = bilin_combine(b, vnw.w, vne.w, vsw.w, vse.w);
+    return o;
+}
+
+// Sum over the slots of one row's table entries; U slots are sampled before accumulating
+// (loads in flight), the additions run in slot order.
+template <int U>
+__device__ __forceinline__ float4 b2_gather_sum4_tab(const float *__restrict__ W, size_t slab,
+                                                      const B2Tap *tab, int n_slots, int nya,
+                                                      int nz, int z) {
+    float4 bp = make_float4(0.f, 0.f, 0.f, 0.f);
+    int s = 0;
+    for (; s + U <= n_slots; s += U) {
+        float4 v[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            const B2Tap t = tab[s + k];
+            v[k] = b2_tap_sample(W + (s + k) * slab, t, nya, nz, z);
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            bp.x = __fadd_rn(bp.x, v[k].x);
+            bp.y = __fadd_rn(bp.y, v[k].y);
+            bp.z = __fadd_rn(bp.z, v[k].z);
+            bp.w = __fadd_rn(bp.w, v[k].w);
+        }
+    }
+    for (; s < n_slots; s++) {
+        const B2Tap t = tab[s];
+        const float4 v = b2_tap_sample(W + s * slab, t, nya, nz, z);
+        bp.x = __fadd_rn(bp.x, v.x);
+        bp.y = __fadd_rn(bp.y, v.y);
+        bp.z = __fadd_rn(bp.z, v.z);
+        bp.w = __fadd_rn(bp.w, v.w);
+    }
+    return bp;
+}
+
+constexpr int kB2Unroll = 2;
+
 template <bool PRIOR>
 __global__ void __launch_bounds__(256)
     k_b2_gather4(SpectDev g, const float *__restrict__ W, const int *__restrict__ alist,
                  int n_slots, float *__restrict__ out, int mode, UpdateArgs u) {
+    __shared__ B2Tap tab[kB2Taps];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int x = blockIdx.z;
     const int N = g.N, nz = g.nz;
+    const int n_rows = blockDim.y;  // a block covers rows y of one plane x
+    const bool use_tab = b2_tab_fits(g, n_rows, n_slots);
+    if (use_tab) {
+        const int nt = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
+        for (int e = tid; e < n_rows * n_slots; e += nt) {
+            const int yr = blockIdx.y * blockDim.y + e / n_slots;
+            if (yr < N) b2_make_tap(g, alist, e % n_slots, x, yr, tab[e]);
+        }
+        __syncthreads();
+    }
     if (4 * q >= nz || y >= N) return;
     const int z = 4 * q;
-    const float4 bp = b2_gather_sum4(g, W, alist, n_slots, x, y, z);
+    const float4 bp = use_tab ? b2_gather_sum4_tab<kB2Unroll>(
+                                    W, (size_t)g.Lp * g.nya * nz, tab + threadIdx.y * n_slots,
+                                    n_slots, g.nya, nz, z)
+                              : b2_gather_sum4(g, W, alist, n_slots, x, y, z);
     const size_t i = ((size_t)x * N + y) * nz + z;
     apply_update4<PRIOR>(mode, u, i, x, y, z, N, N, nz, bp, out);
 }
@@ -824,13 +938,30 @@ int b2_gather_blocks(const SpectDev &g) {
 // Batched reference back-projector with its epilogue: a thread per (x, y, z quad) of an
 // entry's object (nz % 4 == 0), flat over the entry's voxels.
 __global__ void __launch_bounds__(256) k_b2_gather_batch(const __grid_constant__ B2Batch p) {
+    __shared__ B2Tap tab[kB2Taps];
     const int e = batch_entry(p.block_off, blockIdx.x);
     const SpectDev &g = p.g[e];
-    const long long q = (long long)(blockIdx.x - p.block_off[e]) * 256 + threadIdx.x;
-    const int N = g.N, nz = g.nz, nq = nz / 4;
-    if (q >= (long long)N * N * nq) return;
+    const long long q0 = (long long)(blockIdx.x - p.block_off[e]) * 256;
+    const long long q = q0 + threadIdx.x;
+    const int N = g.N, nz = g.nz, nq = nz / 4, ns = p.n_slots[e];
+    const long long total = (long long)N * N * nq;
+    // rows (x N + y) of the block's voxels
+    const long long row0 = q0 / nq;
+    const int n_rows = (int)((min(q0 + 255, total - 1)) / nq - row0) + 1;
+    const bool use_tab = b2_tab_fits(g, n_rows, ns);
+    if (use_tab) {
+        for (int k = threadIdx.x; k < n_rows * ns; k += 256) {
+            const long long row = row0 + k / ns;
+            b2_make_tap(g, p.alist[e], k % ns, (int)(row / N), (int)(row % N), tab[k]);
+        }
+        __syncthreads();
+    }
+    if (q >= total) return;
     const int z = 4 * (int)(q % nq), y = (int)((q / nq) % N), x = (int)(q / ((long long)nq * N));
-    const float4 bp = b2_gather_sum4(g, p.W[e], p.alist[e], p.n_slots[e], x, y, z);
+    const float4 bp =
+        use_tab ? b2_gather_sum4_tab<kB2Unroll>(p.W[e], (size_t)g.Lp * g.nya * nz,
+                                               tab + (int)(q / nq - row0) * ns, ns, g.nya, nz, z)
+                : b2_gather_sum4(g, p.W[e], p.alist[e], ns, x, y, z);
     const size_t i = ((size_t)x * N + y) * nz + z;
     UpdateArgs u{};
     u.f = p.out[e];
