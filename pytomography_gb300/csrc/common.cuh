@@ -53,11 +53,15 @@ inline cudaStream_t as_stream(gb_stream_t s) { return reinterpret_cast<cudaStrea
 enum FaultSite { FAULT_ALLOC = 0, FAULT_LAUNCH = 1, FAULT_ARG = 2, FAULT_SITES = 3 };
 bool fault_injected(FaultSite site);
 
-// cudaMalloc with the allocation fault site in front of it.
-inline cudaError_t dev_alloc(void **p, size_t bytes) {
-    if (fault_injected(FAULT_ALLOC)) return cudaErrorMemoryAllocation;
-    return cudaMalloc(p, bytes);
-}
+// Device memory of plans, batches and their scratch, with the allocation fault site in
+// front of it.  Blocks come from a library-owned stream-ordered pool per device
+// (cudaMemPool) that keeps up to kPoolKeepBytes of freed memory reserved, so a plan
+// created after another was destroyed reuses its memory without new driver mappings.
+// dev_alloc returns memory usable from any stream; dev_free waits for the device first
+// (as cudaFree does), so no kernel in flight can see a block handed out again.
+constexpr unsigned long long kPoolKeepBytes = 16ull << 30;
+cudaError_t dev_alloc(void **p, size_t bytes);
+void dev_free(void *p);
 template <typename T>
 inline cudaError_t dev_alloc(T **p, size_t bytes) {
     return dev_alloc(reinterpret_cast<void **>(p), bytes);

@@ -227,15 +227,15 @@ struct gb_pet_plan {
 
 static void pet_free(gb_pet_plan *p) {
     if (!p) return;
-    cudaFree(p->d_lut);
-    cudaFree(p->d_ev);
-    cudaFree(p->d_ratio);
-    cudaFree(p->d_bp);
-    cudaFree(p->d_rec);
-    cudaFree(p->d_tof_tab);
-    cudaFree(p->d_acc64);
-    cudaFree(p->d_maxbits);
-    cudaFree(p->d_scale);
+    dev_free(p->d_lut);
+    dev_free(p->d_ev);
+    dev_free(p->d_ratio);
+    dev_free(p->d_bp);
+    dev_free(p->d_rec);
+    dev_free(p->d_tof_tab);
+    dev_free(p->d_acc64);
+    dev_free(p->d_maxbits);
+    dev_free(p->d_scale);
     delete p;
 }
 
@@ -256,7 +256,7 @@ static void subset_range(const gb_pet_plan *p, int subset, long long &first, lon
 // equal keys keep list order) and pack the tiles.
 static gb_status build_tiles(gb_pet_plan *p, int n_subsets) {
     const long long E = p->n_events;
-    cudaFree(p->d_rec);
+    dev_free(p->d_rec);
     p->d_rec = nullptr;
     p->list_off.assign(1, 0);
     if (E == 0) {
@@ -270,7 +270,7 @@ static gb_status build_tiles(gb_pet_plan *p, int n_subsets) {
     size_t tmp_bytes = 0;
     cudaError_t e = cudaSuccess;
     auto fail = [&](cudaError_t err) {
-        cudaFree(keys); cudaFree(keys2); cudaFree(vals); cudaFree(vals2); cudaFree(tmp);
+        dev_free(keys); dev_free(keys2); dev_free(vals); dev_free(vals2); dev_free(tmp);
         set_error("event tile build failed: %s", cudaGetErrorString(err));
         return err == cudaErrorMemoryAllocation ? GB_ERR_OOM : GB_ERR_CUDA;
     };
@@ -306,7 +306,7 @@ static gb_status build_tiles(gb_pet_plan *p, int n_subsets) {
         off += n;
     }
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
-    cudaFree(keys); cudaFree(keys2); cudaFree(vals); cudaFree(vals2); cudaFree(tmp);
+    dev_free(keys); dev_free(keys2); dev_free(vals); dev_free(vals2); dev_free(tmp);
     return GB_OK;
 }
 
@@ -479,9 +479,9 @@ gb_status gb_pet_backward(gb_pet_plan *p, const float *proj, float *img, int32_t
 gb_status gb_pet_set_deterministic(gb_pet_plan *p, int32_t on) {
     clear_error();
     GB_CHECK_ARG(p, "null plan");
-    cudaFree(p->d_acc64);
-    cudaFree(p->d_maxbits);
-    cudaFree(p->d_scale);
+    dev_free(p->d_acc64);
+    dev_free(p->d_maxbits);
+    dev_free(p->d_scale);
     p->d_acc64 = nullptr;
     p->d_maxbits = nullptr;
     p->d_scale = nullptr;

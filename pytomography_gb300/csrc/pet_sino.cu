@@ -127,9 +127,9 @@ struct gb_pet_sino_plan {
 
 static void sino_free(gb_pet_sino_plan *p) {
     if (!p) return;
-    cudaFree(p->d_det);
-    cudaFree(p->d_z);
-    cudaFree(p->d_tof_tab);
+    dev_free(p->d_det);
+    dev_free(p->d_z);
+    dev_free(p->d_tof_tab);
     delete p;
 }
 

@@ -56,6 +56,65 @@ static void fault_env_init() {
     }
 }
 
+namespace {
+struct DevicePool {
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t st = nullptr;  // allocation / release stream (non-blocking, library-owned)
+    bool tried = false;
+};
+std::mutex g_pool_mutex;
+DevicePool g_pools[64];
+
+// The pool of the current device, created on first use; null when the device has no
+// memory-pool support (plain cudaMalloc / cudaFree are used then, for every block).
+DevicePool *device_pool() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_pool_mutex);
+    DevicePool &d = g_pools[dev];
+    if (!d.tried) {
+        d.tried = true;
+        int supported = 0;
+        cudaDeviceGetAttribute(&supported, cudaDevAttrMemoryPoolsSupported, dev);
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        if (supported && cudaMemPoolCreate(&d.pool, &props) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&d.st, cudaStreamNonBlocking) == cudaSuccess) {
+            unsigned long long keep = kPoolKeepBytes;
+            cudaMemPoolSetAttribute(d.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        } else {
+            if (d.pool) cudaMemPoolDestroy(d.pool);
+            d.pool = nullptr;
+            d.st = nullptr;
+            cudaGetLastError();
+        }
+    }
+    return d.pool ? &d : nullptr;
+}
+}  // namespace
+
+cudaError_t dev_alloc(void **p, size_t bytes) {
+    if (fault_injected(FAULT_ALLOC)) return cudaErrorMemoryAllocation;
+    DevicePool *d = device_pool();
+    if (!d) return cudaMalloc(p, bytes);
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, d->pool, d->st);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(d->st);  // the block is then usable from every stream
+}
+
+void dev_free(void *p) {
+    if (!p) return;
+    DevicePool *d = device_pool();
+    if (!d) {
+        cudaFree(p);
+        return;
+    }
+    cudaDeviceSynchronize();
+    cudaFreeAsync(p, d->st);
+}
+
 bool fault_injected(FaultSite site) {
     std::call_once(g_fault_env_once, fault_env_init);
     int c = g_fault_countdown[site].load();
@@ -135,15 +194,15 @@ struct gb_spect_plan {
 
 static void free_plan(gb_spect_plan *p) {
     if (!p) return;
-    cudaFree(p->d_lin); cudaFree(p->d_theta_fwd); cudaFree(p->d_theta_bwd);
-    cudaFree(p->d_taps_r); cudaFree(p->d_taps_z); cudaFree(p->d_A); cudaFree(p->d_group);
-    cudaFree(p->d_tier);
-    cudaFree(p->dev.phase);
-    cudaFree(p->d_alist); cudaFree(p->d_items); cudaFree(p->d_ioff);
-    cudaFree(p->d_partials); cudaFree(p->d_W); cudaFree(p->d_ratio);
-    cudaFree(p->d_bp);
-    cudaFree(p->d_wrange);
-    cudaFree(p->d_err);
+    dev_free(p->d_lin); dev_free(p->d_theta_fwd); dev_free(p->d_theta_bwd);
+    dev_free(p->d_taps_r); dev_free(p->d_taps_z); dev_free(p->d_A); dev_free(p->d_group);
+    dev_free(p->d_tier);
+    dev_free(p->dev.phase);
+    dev_free(p->d_alist); dev_free(p->d_items); dev_free(p->d_ioff);
+    dev_free(p->d_partials); dev_free(p->d_W); dev_free(p->d_ratio);
+    dev_free(p->d_bp);
+    dev_free(p->d_wrange);
+    dev_free(p->d_err);
     if (p->st2) cudaStreamDestroy(p->st2);
     if (p->ev_fork) cudaEventDestroy(p->ev_fork);
     if (p->ev_join) cudaEventDestroy(p->ev_join);
@@ -356,9 +415,9 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
         }
         p->lists.push_back(L);
     }
-    cudaFree(p->d_alist);
-    cudaFree(p->d_items);
-    cudaFree(p->d_ioff);
+    dev_free(p->d_alist);
+    dev_free(p->d_items);
+    dev_free(p->d_ioff);
     p->d_alist = nullptr;
     p->d_items = nullptr;
     p->d_ioff = nullptr;
@@ -374,7 +433,7 @@ static gb_status upload_lists(gb_spect_plan *p, int n_subsets) {
     p->lists_version++;
     size_t need = max_items * p->N * p->nz;
     if (need > p->partials_cap) {
-        cudaFree(p->d_partials);
+        dev_free(p->d_partials);
         p->d_partials = nullptr;
         GB_CUDA(dev_alloc(&p->d_partials, need * sizeof(float)));
         p->partials_cap = need;
@@ -860,9 +919,9 @@ gb_status gb_spect_autotune(gb_spect_plan *p, int32_t subset, int32_t reps,
     gb_spect_tuning best{};
     gb_spect_get_tuning(p, &best);
     auto cleanup = [&]() {
-        cudaFree(obj);
-        cudaFree(proj);
-        cudaFree(back);
+        dev_free(obj);
+        dev_free(proj);
+        dev_free(back);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
     };
@@ -1188,21 +1247,21 @@ struct gb_spect_batch {
 static void free_batch(gb_spect_batch *b) {
     if (!b) return;
     for (int e = 0; e < kMaxBatch; e++) {
-        cudaFree(b->wrange[e]);
-        cudaFree(b->W[e]);
-        cudaFree(b->ratio[e]);
-        cudaFree(b->bp[e]);
+        dev_free(b->wrange[e]);
+        dev_free(b->W[e]);
+        dev_free(b->ratio[e]);
+        dev_free(b->bp[e]);
     }
     for (auto &L : b->lists) {
-        cudaFree(L.fitems);
-        cudaFree(L.rows);
-        cudaFree(L.row_off);
-        cudaFree(L.row_items);
-        for (int4 *p : L.bitems) cudaFree(p);
+        dev_free(L.fitems);
+        dev_free(L.rows);
+        dev_free(L.row_off);
+        dev_free(L.row_items);
+        for (int4 *p : L.bitems) dev_free(p);
     }
-    cudaFree(b->partials);
-    cudaFree(b->counters);
-    cudaFree(b->d_alists);
+    dev_free(b->partials);
+    dev_free(b->counters);
+    dev_free(b->d_alists);
     delete b;
 }
 

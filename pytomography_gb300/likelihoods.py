@@ -58,7 +58,10 @@ class Likelihood:
         else:
             sm.set_n_subsets(n_subsets)
             if self._normalisation_split != n_subsets:
-                self.norm_BPs = [sm.compute_normalization_factor(k) for k in range(n_subsets)]
+                if hasattr(sm, "compute_normalization_factors"):
+                    self.norm_BPs = sm.compute_normalization_factors()
+                else:
+                    self.norm_BPs = [sm.compute_normalization_factor(k) for k in range(n_subsets)]
         self._normalisation_split = n_subsets
 
     def _get_normBP(self, subset_idx, return_sum: bool = False):

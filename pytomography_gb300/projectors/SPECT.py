@@ -85,10 +85,11 @@ class SPECTSystemMatrix(SystemMatrix):
                     "transforms must be configured for the system matrix's frame "
                     "(assume_padded=True for SPECTSystemMatrix, False for StarGuide)")
         angles = pm.angles.to(torch.float32).cpu()
-        # forward rotation: RotationTransform.backward(obj, 270 - beta) -> rotate(beta - 270)
-        self._theta_fwd = geometry.rotation_theta(-(270 - angles), Lp)
-        # back-projection rotation: RotationTransform.forward(obj, 270 - beta)
-        self._theta_bwd = geometry.rotation_theta(270 - angles, Lp)
+        # forward rotation: RotationTransform.backward(obj, 270 - beta) -> rotate(beta - 270);
+        # back-projection rotation: RotationTransform.forward(obj, 270 - beta).  One batched
+        # call (every matrix is computed on its own, so the rows are those of two calls).
+        both = geometry.rotation_theta(torch.cat([-(270 - angles), 270 - angles]), Lp)
+        self._theta_fwd, self._theta_bwd = both[:n].contiguous(), both[n:].contiguous()
         self._lin = geometry.base_grid(Lp)
         order = ""
         mu = None
@@ -321,6 +322,26 @@ class SPECTSystemMatrix(SystemMatrix):
         n = self._n_sel(subset_idx)
         ones = torch.ones((n, *self.proj_meta.shape[1:]), device=self.device)
         return self.backward(ones, subset_idx)
+
+    def compute_normalization_factors(self) -> list:
+        """H_m^T 1 of every subset of the current split, in subset order: the values of
+        ``compute_normalization_factor(m)`` for each m, from one buffer of ones and one
+        back-projection call per subset."""
+        if self.subset_indices_array is None:
+            return [self.compute_normalization_factor(None)]
+        n_max = max(len(ix) for ix in self.subset_indices_array)
+        ones = torch.ones((n_max, *self.proj_meta.shape[1:]), device=self.device)
+        st = _lib.stream_handle(self.device)
+        outs = []
+        for k in range(len(self.subset_indices_array)):
+            out = torch.empty(tuple(self.object_meta.shape), device=self.device,
+                              dtype=torch.float32)
+            # the first n_sel(k) rows of the buffer are subset k's projection of ones
+            _lib.check(self._lib.gb_spect_backward(self._plan, _lib.ptr(ones), _lib.ptr(out),
+                                                   k, 0, st))
+            outs.append(out)
+        self._after_call()
+        return outs
 
     # ------------------------------------------------------------ fused updates
     def osem_step(self, object: torch.Tensor, projections: torch.Tensor,

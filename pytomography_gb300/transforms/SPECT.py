@@ -65,11 +65,17 @@ class SPECTAttenuationTransform(Transform):
         n = int(object_meta.shape[0])
         self._pad = geometry.compute_pad_size(n) if self.assume_padded else 0
         self._L = n + 2 * self._pad
-        angles = torch.as_tensor(proj_meta.angles, dtype=torch.float32).reshape(-1).cpu()
-        # the map is sampled with the forward projector's rotation, angle beta - 270
-        # (utils/spatial.py:29-31 through rotate_detector_z)
-        self._theta = geometry.rotation_theta(-(270 - angles), self._L).numpy()
+        self._theta_cache = None  # built on the first per-angle call (fused plans skip it)
         self._dev = None
+
+    @property
+    def _theta(self) -> np.ndarray:
+        if self._theta_cache is None:
+            angles = torch.as_tensor(self.proj_meta.angles, dtype=torch.float32).reshape(-1).cpu()
+            # the map is sampled with the forward projector's rotation, angle beta - 270
+            # (utils/spatial.py:29-31 through rotate_detector_z)
+            self._theta_cache = geometry.rotation_theta(-(270 - angles), self._L).numpy()
+        return self._theta_cache
 
     def _device_tables(self, device):
         if self._dev is None or self._dev[0] != device:
