@@ -37,6 +37,13 @@ const char *gb_last_error(void);
 /* Library version string. */
 const char *gb_version(void);
 
+/* Device memory of plans and batches comes from a library-owned stream-ordered pool on each
+ * device, which keeps up to 16 GiB of freed blocks reserved for the next plan (no
+ * counterpart in the reference, whose tensors come from PyTorch's caching allocator).
+ * Returns the current device's reserved but unused blocks to the driver, after waiting for
+ * the device, so that other allocators can use them; blocks of live plans stay. */
+gb_status gb_release_pool_memory(void);
+
 /* Host-side fault injection for tests of the error paths (no counterpart in the reference,
  * which has no native code).  Arms `site` ("alloc": a device allocation at plan creation,
  * subset setup or tuning returns GB_ERR_OOM; "launch": a projector / update entry point

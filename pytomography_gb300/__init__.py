@@ -35,3 +35,10 @@ def set_device(d):
 def set_verbose(b: bool):
     global verbose
     verbose = b
+
+
+def release_pool_memory() -> None:
+    """Return the device memory that destroyed plans left reserved in the library's pool
+    (up to 16 GiB is kept for the next plan) to the driver, e.g. before PyTorch needs it."""
+    from . import _lib
+    _lib.check(_lib.load().gb_release_pool_memory())

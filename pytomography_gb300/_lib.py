@@ -78,6 +78,7 @@ _LIB = None
 SIGNATURES = [
     ("gb_last_error", c_char_p, []),
     ("gb_version", c_char_p, []),
+    ("gb_release_pool_memory", c_int, []),
     ("gb_spect_plan_create", c_int, [ctypes.POINTER(SpectDesc), ctypes.POINTER(c_void_p)]),
     ("gb_spect_plan_destroy", c_int, [c_void_p]),
     ("gb_spect_set_subsets", c_int, [c_void_p, c_int]),

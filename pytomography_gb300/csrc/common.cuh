@@ -62,6 +62,9 @@ bool fault_injected(FaultSite site);
 constexpr unsigned long long kPoolKeepBytes = 16ull << 30;
 cudaError_t dev_alloc(void **p, size_t bytes);
 void dev_free(void *p);
+// Returns the current device pool's reserved, unused blocks to the driver (after a device
+// synchronize).
+cudaError_t release_pool_memory();
 template <typename T>
 inline cudaError_t dev_alloc(T **p, size_t bytes) {
     return dev_alloc(reinterpret_cast<void **>(p), bytes);

@@ -104,6 +104,14 @@ cudaError_t dev_alloc(void **p, size_t bytes) {
     return cudaStreamSynchronize(d->st);  // the block is then usable from every stream
 }
 
+cudaError_t release_pool_memory() {
+    DevicePool *d = device_pool();
+    if (!d) return cudaSuccess;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return e;
+    return cudaMemPoolTrimTo(d->pool, 0);
+}
+
 void dev_free(void *p) {
     if (!p) return;
     DevicePool *d = device_pool();
@@ -499,6 +507,12 @@ gb_status gb_inject_fault(const char *site, int32_t nth) {
     return GB_OK;
 }
 const char *gb_version(void) { return "gbtomo 0.1.0 (sm_103a)"; }
+
+gb_status gb_release_pool_memory(void) {
+    clear_error();
+    GB_CUDA(release_pool_memory());
+    return GB_OK;
+}
 
 gb_status gb_spect_plan_create(const gb_spect_desc *d, gb_spect_plan **out) {
     clear_error();

@@ -60,3 +60,19 @@ def test_bounded_wait_runs_out_and_reports(cuda):
     out = H.forward(f)
     assert H.device_status() == 0
     assert rel_l2(out.cpu().numpy(), d["fwd_att+psf_f32"]) < 1e-5
+
+
+def test_pool_memory_release_keeps_live_plans_usable(cuda):
+    """Destroyed plans' blocks go back to the driver; a live plan still projects correctly
+    and a new plan can be built afterwards."""
+    import gc
+    import pytomography_gb300 as p
+    d, H, f = _sm(cuda)
+    ref = H.forward(f)
+    _, H2, _ = _sm(cuda)
+    del H2
+    gc.collect()
+    p.release_pool_memory()
+    assert torch.equal(H.forward(f), ref)
+    _, H3, _ = _sm(cuda)
+    assert torch.equal(H3.forward(f), ref)

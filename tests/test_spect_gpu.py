@@ -150,3 +150,43 @@ def test_full_size_geometries_vs_oracle(n, nz, n_angles, order, radius, dr, cuda
     adj = H.backward_adjoint(torch.tensor(g, dtype=torch.float32, device=cuda), sub).cpu().numpy()
     assert rel_l2(adj, o.adjoint(g, idx)) < TOL
     assert H.device_status() == 0
+
+
+@pytest.mark.parametrize("n_sub", [1, 2])
+def test_back_projection_sample_table_and_fallback_vs_oracle(n_sub, cuda):
+    """16 x 16 x 16 with 10 angles: a gather block covers 64 rows (4 z quads per row), so
+    one subset of 10 angles (640 row-angle pairs) takes the per-thread sample form and two
+    subsets of 5 (320 pairs) the shared per-block table; both against the oracle."""
+    from pytomography_gb300.metadata.SPECT import SPECTObjectMeta, SPECTProjMeta, SPECTPSFMeta
+    from pytomography_gb300.projectors.SPECT import SPECTSystemMatrix
+    from pytomography_gb300.transforms.SPECT import SPECTAttenuationTransform, SPECTPSFTransform
+    n, nz, n_angles, dr, radius = 16, 16, 10, 0.5, 15.0
+    f, mu, angles = _synthetic(n, nz, n_angles, seed=7)
+    om = SPECTObjectMeta([dr] * 3, (n, n, nz))
+    pm = SPECTProjMeta((n, nz), [dr] * 2, list(angles), radii=[radius] * n_angles)
+    H = SPECTSystemMatrix([SPECTAttenuationTransform(torch.tensor(mu, dtype=torch.float32)),
+                           SPECTPSFTransform(SPECTPSFMeta((0.03, 0.11)))], [], om, pm)
+    o = oracle.SpectOracle((n, n, nz), (dr,) * 3, angles, [radius] * n_angles, mu=mu,
+                           psf=(0.03, 0.11), order="ap")
+    rng = np.random.default_rng(3)
+    if n_sub == 1:
+        g = rng.random((n_angles, n, nz)) * 3
+        bwd = H.backward(torch.tensor(g, dtype=torch.float32, device=cuda)).cpu().numpy()
+        assert rel_l2(bwd, o.backward(g, None)) < TOL
+        return
+    H.set_n_subsets(n_sub)
+    for k in range(n_sub):
+        idx = H.subset_indices_array[k].cpu().numpy()
+        g = rng.random((len(idx), n, nz)) * 3
+        bwd = H.backward(torch.tensor(g, dtype=torch.float32, device=cuda), k).cpu().numpy()
+        assert rel_l2(bwd, o.backward(g, idx)) < TOL, k
+
+
+def test_normalization_factors_in_one_call_match_per_subset(cuda):
+    d = golden("spect_even")
+    H = make_sm(d, "att+psf", cuda)
+    H.set_n_subsets(3)
+    many = H.compute_normalization_factors()
+    assert len(many) == 3
+    for k in range(3):
+        assert torch.equal(many[k], H.compute_normalization_factor(k)), k
