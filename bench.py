@@ -211,6 +211,44 @@ class CpuSubiter:
         return time.perf_counter() - t0
 
 
+def fma_cobound(w, n_sel: int, launch_ms: float, dev):
+    """The PSF blur's FLOP model of the forward launch (2 P (K_r + K_z) per angle, P = the
+    padded volume, full taps at every plane) against the nominal FP32 FMA peak of the device
+    (SMs x 128 lanes x 2 FLOP x the maximum SM clock); None without PSF."""
+    if not w.psf:
+        return None
+    import torch
+    from pytomography_gb300 import geometry
+    n, nz = w.shape[0], w.shape[2]
+    lp = n + 2 * geometry.compute_pad_size(n)
+    sig = geometry.psf_sigma(lp, w.radius, w.dr[0], _PsfFit(w.psf))
+    k = geometry.psf_kernel_size(sig, w.dr[0], 3.0)
+    flops = 2.0 * lp * lp * nz * (2 * k) * n_sel
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = 2070.0
+    try:
+        with open(PEAKS) as fh:
+            mhz = float(json.load(fh).get("sm_max_mhz", mhz))
+    except (OSError, ValueError):
+        pass
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    ach = flops / (launch_ms / 1000) / 1e12
+    return {"flops_per_launch": flops, "taps": k, "achieved_tflops": ach, "peak_tflops": peak,
+            "frac": ach / peak, "peak_kind": f"nominal: {sms} SMs x 128 FP32 lanes x 2 FLOP x "
+                                             f"{mhz:.0f} MHz"}
+
+
+class _PsfFit:
+    """sigma(d) = a d + b, the PSF model of the workloads (cm)."""
+
+    def __init__(self, ab):
+        self.sigma_fit_params = tuple(ab)
+
+    @staticmethod
+    def sigma_fit(d, a, b):
+        return a * d + b
+
+
 def osem_config(w, n_sub: int, n_sel: int, world: int) -> dict:
     """The ``config`` of an OSEM workload's line; both arms print the same one."""
     return {"workload": w.name, "subsets": n_sub, "angles_per_step": n_sel,
@@ -691,7 +729,8 @@ def run_osem(args, dev, w, rank, world, dist, full=True):
                          "traffic_source": "constant from a separate ncu capture of one "
                                            "launch (dram__bytes_read.sum + "
                                            "dram__bytes_write.sum); not measured by this run",
-                         "alg_bytes_per_launch": fwd_bytes, "launch_ms": fwd_ms},
+                         "alg_bytes_per_launch": fwd_bytes, "launch_ms": fwd_ms,
+                         "fma_cobound": fma_cobound(w, n_sel, fwd_ms, dev)},
             "backward_ms": bwd_ms,
             "alg_gbs_per_subiter": sub_bytes / (fused_ms / 1000) / 1e9,
             "gpu_launches": 4 * args.steps,
