@@ -213,6 +213,8 @@ class SPECTSystemMatrix(SystemMatrix):
 
     # ------------------------------------------------------------ subsets
     def set_n_subsets(self, n_subsets: int) -> None:
+        if self.subset_indices_array is not None and int(n_subsets) == self.n_subsets:
+            return  # the same split: indices and the plan's work lists are unchanged
         indices = torch.arange(self.proj_meta.shape[0]).to(torch.long).to(self.device)
         self.subset_indices_array = [indices[i::n_subsets] for i in range(n_subsets)]
         self.n_subsets = n_subsets
