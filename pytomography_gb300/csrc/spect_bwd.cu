@@ -184,6 +184,9 @@ __device__ __forceinline__ void b1_psf_item(const SpectDev &g, const float *__re
 #pragma unroll
     for (int k = 0; k < 6; k++) th[k] = g.theta_fwd[6 * ga + k];
     int parity = 0;
+    // plane whose taps the end of the previous plane stored in tp[parity] (-1: none); the
+    // taps of plane xp + 1 are loaded during plane xp, so the y blur does not wait for them
+    int taps_of = -1;
 #ifdef GB_PHASE_TIMING
     unsigned long long tacc[16] = {};
     const long long t_start = clock64();
@@ -202,7 +205,7 @@ __device__ __forceinline__ void b1_psf_item(const SpectDev &g, const float *__re
         const int o_lo = ra - (g.pad - H), o_hi = rb - (g.pad - H) + 1;  // output rows
         const int b_lo = o_lo / OB, b_hi = (o_hi + OB - 1) / OB;
         float *tap = tp + parity * 2 * K;
-        if (threadIdx.x < K) {
+        if (taps_of != xp && threadIdx.x < K) {
             tap[threadIdx.x] = g.taps_r[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x];
             tap[K + threadIdx.x] =
                 g.psf2d ? g.taps_z[((size_t)grp * g.Lp + xp) * g.K + threadIdx.x] : 0.f;
@@ -226,6 +229,14 @@ __device__ __forceinline__ void b1_psf_item(const SpectDev &g, const float *__re
             long long t1 = GB_B1NOW();
             GB_B1T(2, t1 - t0);
             t0 = t1;
+        }
+        // the next plane's taps: loaded now, stored after this plane's z pass into the other
+        // buffer (free: every warp has passed this plane's first barrier)
+        const bool pre = xp + 1 < x1 && threadIdx.x < K;
+        float nt_r = 0.f, nt_z = 0.f;
+        if (pre) {
+            nt_r = g.taps_r[((size_t)grp * g.Lp + xp + 1) * g.K + threadIdx.x];
+            if (g.psf2d) nt_z = g.taps_z[((size_t)grp * g.Lp + xp + 1) * g.K + threadIdx.x];
         }
         int tier = kTiers - 1;
         if constexpr (FIXED) tier = g.tier ? g.tier[grp * g.Lp + xp] : kTiers - 1;
@@ -329,6 +340,12 @@ __device__ __forceinline__ void b1_psf_item(const SpectDev &g, const float *__re
                 }
             });
         }
+        if (pre) {
+            float *nt = tp + (parity ^ 1) * 2 * K;
+            nt[threadIdx.x] = nt_r;
+            nt[K + threadIdx.x] = nt_z;
+        }
+        taps_of = xp + 1;
         {
             long long t1 = GB_B1NOW();
             GB_B1T(5, t1 - t0);

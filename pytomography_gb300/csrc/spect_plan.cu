@@ -252,17 +252,19 @@ static bool host_plane_rows(const gb_spect_plan *p, int a, int xp, int ylo, int 
     return ra <= rb;
 }
 
-// Estimated cost (SM cycles) of every plane of angle a, a linear model fitted to
-// per-CTA cycle counts of both kernels on GB300 (object sizes 64-128, 60-120 angles,
-// three subsets each): a fixed cost per occupied plane (barriers, pipeline drain), a cost
-// per sampled row and a cost per blurred output row and tap (the plane's tap tier sets
-// the taps).
+// Estimated cost (SM cycles) of every plane of angle a, linear models fitted to per-CTA
+// cycle counts on GB300 (object sizes 64-128, 60-120 angles, three subsets each): a fixed
+// cost per occupied plane (barriers, pipeline drain), a cost per sampled row and a cost
+// per blurred output row and tap (the plane's tap tier sets the taps).
 //   forward: 6360 + 106 rows + 2.76 (output rows x taps); a plane no sample reaches: 100
-//   B1:      4470 +  97 rows + 2.64 (rows x taps);        a plane no sample reaches: 600
+//   B1:      5370 +  67 rows + 2.37 (rows x taps);        a plane no sample reaches: 835
+// (B1's model was refitted by least squares, with a constant per CTA that the split does
+// not need, after its z-pass tasks changed shape; the forward's refit the same way moved
+// the launch from 0.1622 to 0.1641 ms and was not kept.)
 // (The forward skips empty planes with a support test; B1 also records their empty row
 // range.)
 static std::vector<double> plane_work(const gb_spect_plan *p, int a, bool fwd) {
-    std::vector<double> w(p->Lp, fwd ? 100.0 : 600.0);
+    std::vector<double> w(p->Lp, fwd ? 100.0 : 835.0);
     const int H = p->H, K = p->dev.K;
     const int ylo = std::max(0, p->pad - H), yhi = std::min(p->Lp, p->pad + p->N + H);
     const int grp = p->h_group.empty() ? 0 : p->h_group[a];
@@ -276,7 +278,7 @@ static std::vector<double> plane_work(const gb_spect_plan *p, int a, bool fwd) {
             const int o = std::min(p->N, rb + H - p->pad + 1) - std::max(0, ra - H - p->pad);
             w[xp] = 6360.0 + 106.0 * rows + 2.76 * kk * std::max(0, o);
         } else {
-            w[xp] = 4470.0 + 97.0 * rows + 2.64 * kk * rows;
+            w[xp] = 5370.0 + 67.0 * rows + 2.37 * kk * rows;
         }
     }
     return w;
