@@ -147,9 +147,14 @@ class SPECTPSFTransform(Transform):
             kz = self._compute_kernel_size(radius, 2)
             sigma = self._get_sigma(radius)
             wr = geometry.psf_taps(sigma / self.object_meta.dx, kr, self.psf_meta.shape)
-            wz = geometry.psf_taps(sigma / self.object_meta.dz, kz, self.psf_meta.shape)
             two_d = self.psf_meta.kernel_dimensions == "2D"
-            self.tables[radius] = (wr, wz if two_d else None)
+            if not two_d:
+                wz = None
+            elif kz == kr and float(self.object_meta.dz) == float(self.object_meta.dx):
+                wz = wr  # cubic voxels: the same arguments give the same taps
+            else:
+                wz = geometry.psf_taps(sigma / self.object_meta.dz, kz, self.psf_meta.shape)
+            self.tables[radius] = (wr, wz)
         self._dev_tables = {}
 
     def _taps_on(self, radius: float, device):

@@ -114,3 +114,23 @@ def test_batched_autograd_matches_object_by_object(cuda):
     p = project(x.detach(), H, 1)
     for b in range(3):
         assert rel_l2(p[b].cpu().numpy(), H.forward(x[b].detach(), 1).cpu().numpy()) < TOL
+
+
+@pytest.mark.parametrize("n_subsets", [1, 10])
+def test_batch_gather_sample_forms(n_subsets, cuda):
+    """16^3 plans with 40 angles: a block of the batched gather covers 65 rows (4 z quads
+    per row), so 16 angle slots per group exceed the per-block sample table (one subset)
+    and 4 slots fit it (ten subsets); both forms against each plan's own back projector."""
+    from pytomography_gb300.batched import SpectBatch, common_psf_bucket
+    ws, Hs, gs = _recons(cuda, seed=17, n=2, sizes=(16,), angle_counts=(40,))
+    common_psf_bucket(Hs)
+    for H in Hs:
+        H.set_n_subsets(n_subsets)
+    b = SpectBatch(Hs)
+    sub = None if n_subsets == 1 else 3
+    rng = np.random.default_rng(2)
+    gp = [torch.tensor(rng.random((H._n_sel(sub), 16, 16)), dtype=torch.float32, device=cuda)
+          for H in Hs]
+    back = b.backward(gp, sub)
+    for H, g, o in zip(Hs, gp, back):
+        assert rel_l2(o.cpu().numpy(), H.backward(g, sub).cpu().numpy()) < TOL

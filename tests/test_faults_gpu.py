@@ -76,3 +76,19 @@ def test_pool_memory_release_keeps_live_plans_usable(cuda):
     assert torch.equal(H.forward(f), ref)
     _, H3, _ = _sm(cuda)
     assert torch.equal(H3.forward(f), ref)
+
+
+def test_plan_churn_reuses_pool_memory(cuda):
+    """Creating and destroying the same plan repeatedly reuses the pool's blocks: after the
+    first round the device's free memory does not shrink further."""
+    import gc
+    torch.cuda.synchronize()
+    free = []
+    for _ in range(6):
+        d, H, f = _sm(cuda)
+        H.forward(f)
+        del H
+        gc.collect()
+        torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
+    assert min(free[1:]) >= free[0] - (64 << 20), free
