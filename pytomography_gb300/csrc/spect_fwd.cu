@@ -124,45 +124,6 @@ __global__ void k_reduce(const int *__restrict__ ioff, int NZ, const float *__re
     out[o] = gproj[gi] / (pr + kDelta);
 }
 
-// k_reduce over four consecutive outputs per thread (NZ % 4 == 0, every buffer 16-byte
-// aligned): 16-byte loads and stores, each component added in the same item order as
-// k_reduce, so the results are the same.
-__device__ __forceinline__ float4 add4(float4 a, float4 b) {
-    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
-}
-__global__ void k_reduce4(const int *__restrict__ ioff, int NZ, const float *__restrict__ partials,
-                          float *__restrict__ out, int ratio, const float *__restrict__ gproj,
-                          const float *__restrict__ sadd, const int *__restrict__ alist,
-                          float *__restrict__ pred) {
-    const int slot = blockIdx.y;
-    const int i = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-    if (i >= NZ) return;
-    const int c0 = ioff[slot], c1 = ioff[slot + 1];
-    auto part = [&](int c) {
-        return __ldg(reinterpret_cast<const float4 *>(partials + (size_t)c * NZ + i));
-    };
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    int c = c0;
-    for (; c + 4 <= c1; c += 4) {  // four partials' loads in flight, added in item order
-        const float4 p0 = part(c), p1 = part(c + 1), p2 = part(c + 2), p3 = part(c + 3);
-        v = add4(add4(add4(add4(v, p0), p1), p2), p3);
-    }
-    for (; c < c1; c++) v = add4(v, part(c));
-    const size_t o = (size_t)slot * NZ + i;
-    if (!ratio) {
-        *reinterpret_cast<float4 *>(out + o) = v;
-        return;
-    }
-    const size_t gi = (size_t)alist[slot] * NZ + i;
-    float4 pr = v;
-    if (sadd) pr = add4(v, __ldg(reinterpret_cast<const float4 *>(sadd + gi)));
-    if (pred) *reinterpret_cast<float4 *>(pred + o) = pr;
-    const float4 gv = __ldg(reinterpret_cast<const float4 *>(gproj + gi));
-    *reinterpret_cast<float4 *>(out + o) =
-        make_float4(gv.x / (pr.x + kDelta), gv.y / (pr.y + kDelta), gv.z / (pr.z + kDelta),
-                    gv.w / (pr.w + kDelta));
-}
-
 // Batched reduction: one row (entry, slot) per grid row; the items of the row are added
 // in plane order (the order of row_items), so results do not depend on the work queue.
 __global__ void k_reduce_batch(const __grid_constant__ ReduceBatch p) {
@@ -312,13 +273,6 @@ cudaError_t launch_fwd(const SpectDev &g, const float *f, const int *alist, cons
 cudaError_t launch_reduce(int n_slots, const int *ioff, int NZ, const float *partials, float *out,
                           int ratio, const float *gproj, const float *sadd, const int *alist,
                           float *pred, cudaStream_t st) {
-    auto a16 = [](const void *q) { return ((uintptr_t)q & 15) == 0; };
-    if (NZ % 4 == 0 && a16(partials) && a16(out) && a16(gproj) && a16(sadd) && a16(pred)) {
-        dim3 grid((NZ / 4 + 255) / 256, n_slots);
-        k_reduce4<<<grid, 256, 0, st>>>(ioff, NZ, partials, out, ratio, gproj, sadd, alist,
-                                        pred);
-        return cudaGetLastError();
-    }
     dim3 grid((NZ + 255) / 256, n_slots);
     k_reduce<<<grid, 256, 0, st>>>(ioff, NZ, partials, out, ratio, gproj, sadd, alist, pred);
     return cudaGetLastError();
