@@ -506,6 +506,23 @@ def plugins_case(out):
     print("wrote plugins", L)
 
 
+def camera_path_case(out):
+    """SPECTSystemMatrix._get_object_initial with object_initial_based_on_camera_path
+    (spect_system_matrix.py:38-56): ones, zeroed in every angle's rotated frame behind the
+    camera orbit (radii smaller than half the object width)."""
+    shape, dr = (16, 16, 8), (0.5, 0.5, 0.5)
+    angles = [0.0, 40.0, 95.0, 150.0, 200.0, 245.0, 300.0, 330.0]
+    radii = [3.6, 2.6, 3.1, 2.4, 3.9, 2.9, 4.6, 2.2]
+    om = SPECTObjectMeta(list(dr), shape)
+    pm = SPECTProjMeta((shape[1], shape[2]), list(dr[:2]), list(angles), radii=list(radii))
+    H = SPECTSystemMatrix([], [], om, pm, object_initial_based_on_camera_path=True)
+    init = H._get_object_initial(device="cpu").numpy()
+    np.savez_compressed(os.path.join(out, "camera_path.npz"), shape=np.array(shape),
+                        dr=np.array(dr), angles=np.array(angles), radii=np.array(radii),
+                        object_initial=init)
+    print("wrote camera_path", float(init.mean()))
+
+
 CASES = {}
 
 
@@ -514,9 +531,10 @@ def main():
     only = set(sys.argv[1:])
     if only:
         for name in sorted(only):
-            {"plugins": plugins_case}[name](out)
+            {"plugins": plugins_case, "camera_path": camera_path_case}[name](out)
         return
     plugins_case(out)
+    camera_path_case(out)
     autograd_case(out)
     theta_case(out)
     torch.manual_seed(0)

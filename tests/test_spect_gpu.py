@@ -190,3 +190,20 @@ def test_normalization_factors_in_one_call_match_per_subset(cuda):
     assert len(many) == 3
     for k in range(3):
         assert torch.equal(many[k], H.compute_normalization_factor(k)), k
+
+
+def test_object_initial_on_camera_path_matches_reference(cuda):
+    """_get_object_initial with object_initial_based_on_camera_path against the reference's
+    own mask (spect_system_matrix.py:38-56, fixture tests/golden/camera_path.npz)."""
+    from pytomography_gb300.metadata.SPECT import SPECTObjectMeta, SPECTProjMeta
+    from pytomography_gb300.projectors.SPECT import SPECTSystemMatrix
+    d = golden("camera_path")
+    shape = tuple(int(s) for s in d["shape"])
+    om = SPECTObjectMeta([float(x) for x in d["dr"]], shape)
+    pm = SPECTProjMeta(shape[1:], [float(x) for x in d["dr"][:2]],
+                       [float(a) for a in d["angles"]], radii=[float(r) for r in d["radii"]])
+    H = SPECTSystemMatrix([], [], om, pm, object_initial_based_on_camera_path=True)
+    init = H._get_object_initial().cpu().numpy()
+    ref = d["object_initial"]
+    assert rel_l2(init, ref) < TOL
+    assert np.abs(init - ref).max() < 1e-5
