@@ -506,6 +506,33 @@ def plugins_case(out):
     print("wrote plugins", L)
 
 
+def pet_fov_case(out):
+    """PETLMSystemMatrix._get_object_initial and _get_prior_FOV_scale
+    (petlm_system_matrix.py:59-89) for the small scanner of pet_meta and a 40 x 36 x 16
+    image at 2 mm: the axial field of view zeroes / tapers the outer z slices.  The
+    methods only read the object and scanner geometry, so they run on a stand-in instance
+    (the constructor would compute a sensitivity image through parallelproj)."""
+    from types import SimpleNamespace
+    from pytomography.metadata import ObjectMeta
+    from pytomography.projectors.PET import PETLMSystemMatrix
+    set_precision(torch.float32)
+    info = dict(crystalTransNr=1, crystalTransSpacing=4.0, submoduleTransNr=1,
+                submoduleTransSpacing=0.0, moduleTransNr=1, moduleTransSpacing=0.0,
+                rsectorTransNr=60, crystalAxialNr=8, crystalAxialSpacing=4.0,
+                submoduleAxialNr=1, submoduleAxialSpacing=0.0, moduleAxialNr=1,
+                moduleAxialSpacing=0.0, rsectorAxialNr=1, radius=120.0,
+                firstCrystalAxis=1, NrCrystalsPerRing=60, NrRings=8)
+    lut = pet_shared.get_scanner_LUT(info)
+    shape, dr = (40, 36, 16), (2.0, 2.0, 2.0)
+    me = SimpleNamespace(object_meta=ObjectMeta(list(dr), shape),
+                         proj_meta=SimpleNamespace(scanner_lut=lut), FOV_scale_enabled=True)
+    init = PETLMSystemMatrix._get_object_initial(me, device="cpu").numpy()
+    fov = PETLMSystemMatrix._get_prior_FOV_scale(me).cpu().numpy()
+    np.savez_compressed(os.path.join(out, "pet_fov.npz"), shape=np.array(shape),
+                        dr=np.array(dr), object_initial=init, fov_scale=fov)
+    print("wrote pet_fov", float(init.mean()), float(fov.mean()))
+
+
 def camera_path_case(out):
     """SPECTSystemMatrix._get_object_initial with object_initial_based_on_camera_path
     (spect_system_matrix.py:38-56): ones, zeroed in every angle's rotated frame behind the
@@ -531,10 +558,12 @@ def main():
     only = set(sys.argv[1:])
     if only:
         for name in sorted(only):
-            {"plugins": plugins_case, "camera_path": camera_path_case}[name](out)
+            {"plugins": plugins_case, "camera_path": camera_path_case,
+             "pet_fov": pet_fov_case}[name](out)
         return
     plugins_case(out)
     camera_path_case(out)
+    pet_fov_case(out)
     autograd_case(out)
     theta_case(out)
     torch.manual_seed(0)

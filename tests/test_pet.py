@@ -219,3 +219,16 @@ def test_listmode_osem_step_vs_oracle(cuda):
     assert mask.mean() > 0.3
     assert rel_l2(res[True][mask], f[mask]) < TOL
     assert rel_l2(res[True], res[False]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_object_initial_and_fov_scale_match_reference(cuda):
+    """_get_object_initial and _get_prior_FOV_scale against the reference's own methods
+    (petlm_system_matrix.py:59-89; fixture tests/golden/pet_fov.npz) on the same scanner
+    and image grid."""
+    d = golden("pet_fov")
+    H, _, _, _ = _setup(True, n_events=100, shape=tuple(int(s) for s in d["shape"]),
+                        vox=tuple(float(v) for v in d["dr"]))
+    assert np.array_equal(H._get_object_initial().cpu().numpy(), d["object_initial"])
+    assert np.allclose(H._get_prior_FOV_scale().cpu().numpy(), d["fov_scale"], rtol=0,
+                       atol=1e-6)
